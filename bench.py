@@ -1,0 +1,392 @@
+#!/usr/bin/env python
+"""Benchmark of the Flash-SD-KDE hot path on GB300.
+
+Workload (one step): one-step empirical SD-KDE followed by KDE evaluation,
+d = 16, FP32 inputs: n_train = 65536 points from the 8-component Gaussian
+mixture (weights Dirichlet(1), means N(0, 4I), covariances A A^T/16 + 0.1 I)
+and 65536 fresh mixture queries; bandwidth by Silverman's rule.  A step is
+  empirical score (pdf_sum, weighted_sum; n^2 pair evaluations)
+  + debias shift + KDE of the debiased set at the queries (n*m pairs).
+Metric: exact 16-D pair evaluations per second.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl fsk|reference]
+
+value      device-resident inputs, per-step CUDA events on the launching
+           stream, L2 flushed (256 MiB write) before every timed step.
+e2e        the same step through the public API (emp_sd_kde_fit_transform +
+           kde_eval) from pinned host buffers, H2D and D2H inside the timing.
+roofline   the dominant kernel's pair-evals/s (library timer: CUDA events on
+           its own stream) against the exp-bound peak built from the SFU
+           ex2 and FP32 FMA rates measured on this GPU.
+cpu_baseline  the reference CPU path (numpy restatement) on a bounded
+           sample with all host cores, in a subprocess.
+Multi-GPU (torchrun): every rank runs an independent replica (own query
+set, shared training set); value = all ranks' pairs / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path[:0] = [str(ROOT / "flash-sd-kde_gb300"), str(ROOT)]
+
+N_TRAIN = 65536
+N_QUERY = 65536
+EPS = 1e-12
+# FP32-pipe lane operations per pair in the tensor-core KDE epilogue besides
+# the exp (scale-add, query offset, accumulate) and per polynomial exp2; used
+# for the exp-bound peak P = R_sfu / (1 - f*), f* = (R_fma - c R_sfu) / (R_fma + k R_sfu).
+C_OPS_PER_PAIR = 3.0
+K_OPS_PER_POLY_EXP = 10.0
+KERNEL_NAMES = {1: "kde16_tc_kernel", 2: "kde16_simt_kernel", 3: "score16_simt_kernel",
+                4: "score16_sym_simt_kernel", 5: "kde1d_kernel", 6: "kde1d_score_kernel",
+                7: "score16_tc_kernel", 8: "score16_sym_tc_kernel"}
+
+
+def parse():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["fsk", "reference"], default="fsk")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def metric_name() -> str:
+    return "16D pair-evals/s exact (SD-KDE: empirical score + debias + KDE)"
+
+
+def workload_config() -> dict:
+    return {
+        "workload": "sdkde_gmm8_16d_n65536_m65536",
+        "n_train": N_TRAIN,
+        "n_query": N_QUERY,
+        "d": 16,
+        "bandwidth": "silverman",
+        "pairs_per_step": N_TRAIN * N_TRAIN + N_TRAIN * N_QUERY,
+        "l2": "flushed before each timed step (256 MiB write)",
+        "precision_mode": "fast_tf32 (bf16x3 tensor-core distances + exact FP32 near-pair recompute)",
+    }
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline / reference arm
+# ---------------------------------------------------------------------------
+def cpu_baseline(target_seconds: float, steps: int = 1) -> dict:
+    cmd = [sys.executable, "-m", "oracle.cpu_baseline", "--n", str(N_TRAIN),
+           "--target-seconds", str(target_seconds), "--steps", str(steps)]
+    env = dict(os.environ, OMP_NUM_THREADS="1", OPENBLAS_NUM_THREADS="1", MKL_NUM_THREADS="1")
+    res = subprocess.run(cmd, cwd=str(ROOT), capture_output=True, text=True, env=env, timeout=900)
+    if res.returncode != 0:
+        raise RuntimeError(f"cpu baseline failed: {res.stderr[-2000:]}")
+    return json.loads(res.stdout.strip().splitlines()[-1])
+
+
+def run_reference_arm(args) -> None:
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    warm = cpu_baseline(2.0, steps=max(1, min(args.warmup, 1)))
+    t0 = time.perf_counter()
+    res = cpu_baseline(6.0, steps=args.steps)
+    wall = time.perf_counter() - t0
+    pairs_step = res["value"] * res["seconds"] / args.steps
+    line = {
+        "impl": "reference",
+        "metric": metric_name(),
+        "value": res["value"],
+        "unit": "pair-evals/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * res["seconds"] / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded 8-component Gaussian mixture)",
+        "config": workload_config(),
+        "cpu_baseline": {"value": res["value"], "unit": "pair-evals/s", "cores": res["cores"],
+                         "kind": res["kind"], "sample": res["sample"]},
+        "e2e": {"value": res["value"], "unit": "pair-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "notes": f"each step is a bounded sample of {pairs_step:.3e} pair evaluations of the workload; "
+                 f"warm-up {warm['seconds']:.1f}s, timed wall {wall:.1f}s",
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"fsk_clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self) -> dict:
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        self.path.unlink(missing_ok=True)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def exp_peak(rates) -> dict:
+    r_sfu, r_fma = float(rates[0]), float(rates[1])
+    c, k = C_OPS_PER_PAIR, K_OPS_PER_POLY_EXP
+    f = (r_fma - c * r_sfu) / (r_fma + k * r_sfu)
+    peak = r_sfu / (1.0 - f) if f > 0 else min(r_sfu, r_fma / c)
+    return {"peak": peak, "r_sfu": r_sfu, "r_fma": r_fma, "r_ffma2_lanes": float(rates[2]), "offload_fraction": max(f, 0.0)}
+
+
+def run_gpu_arm(args) -> None:
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    world, rank, local = dist_env()
+    if world > 1:
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", rank=rank, world_size=world)
+    dev = torch.device("cuda", local if world > 1 else 0)
+    torch.cuda.set_device(dev)
+
+    import __graft_entry__ as ge
+
+    ge.build()
+    from flash_sd_kde import emp_sd_kde_fit_transform, kde_eval
+    from fsk import _lib, ops, workloads
+    from oracle import fp64
+
+    lib = _lib.load()
+    gmm = workloads.GMM16(seed=0)
+    x_np = gmm.sample(N_TRAIN, seed=1)
+    q_np = gmm.sample(N_QUERY, seed=2 + rank)
+    x = torch.from_numpy(x_np).to(dev)
+    q = torch.from_numpy(q_np).to(dev)
+    h = float(ops.silverman(x).item())
+    norm = 1.0 / ((2.0 * math.pi) ** 8 * h ** 16 * N_TRAIN)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        pdf, w = ops.empscore16(x, h, variant="ordered")
+        deb = ops.debias16(x, pdf, w, h, EPS)
+        return deb, ops.kde16_sum(q, deb, h, out_scale=norm)
+
+    rates = np.zeros(3)
+    _lib.check(lib.fsk_diag_pipe_rates(rates.ctypes.data, stream.cuda_stream), "pipe rates")
+    peak = exp_peak(rates)
+
+    for _ in range(args.warmup):
+        step()
+    ops.device_status(dev)
+
+    # ---- device-resident timing -------------------------------------------------
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    launches0 = lib.fsk_launch_count()
+    lib.fsk_timer_enable(1)
+    sampler = ClockSampler(dev.index or 0)
+    with sampler:
+        for s_ev, e_ev in evs:
+            flush.zero_()
+            s_ev.record(stream)
+            deb, dens = step()
+            e_ev.record(stream)
+        torch.cuda.synchronize(dev)
+    lib.fsk_timer_enable(0)
+    launches = lib.fsk_launch_count() - launches0
+    step_ms = [s.elapsed_time(e) for s, e in evs]
+    total_ms = float(sum(step_ms))
+    ids = np.zeros(16, np.int32)
+    nl = np.zeros(16, np.int64)
+    kms = np.zeros(16)
+    kwork = np.zeros(16)
+    rows = lib.fsk_timer_collect(ids.ctypes.data, nl.ctypes.data, kms.ctypes.data, kwork.ctypes.data, 16)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        dist.barrier()
+    ops.device_status(dev)
+    pairs_step = float(N_TRAIN) * N_TRAIN + float(N_TRAIN) * N_QUERY
+    value = world * pairs_step * args.steps / (total_ms * 1e-3)
+
+    kernels = {}
+    for r in range(max(rows, 0)):
+        name = KERNEL_NAMES.get(int(ids[r]), str(int(ids[r])))
+        kernels[name] = {"launches": int(nl[r]), "ms": float(kms[r]), "pair_evals": float(kwork[r]),
+                         "pair_evals_per_s": float(kwork[r]) / (kms[r] * 1e-3) if kms[r] > 0 else None,
+                         "share_of_step_time": float(kms[r]) / total_ms if total_ms > 0 else None}
+    dom = max(kernels, key=lambda k: kernels[k]["ms"]) if kernels else None
+    achieved = kernels[dom]["pair_evals_per_s"] if dom else None
+    traffic = None
+    tfile = ROOT / "profiles" / "traffic.json"
+    if dom and tfile.exists():
+        try:
+            traffic = json.loads(tfile.read_text()).get(dom, {}).get("bytes_per_launch")
+        except ValueError:
+            traffic = None
+
+    # ---- end-to-end through the public API from host buffers ----------------------
+    x_pin = torch.from_numpy(x_np).pin_memory()
+    q_pin = torch.from_numpy(q_np).pin_memory()
+    out_pin = torch.empty(N_QUERY, dtype=torch.float32).pin_memory()
+    e2e_evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+
+    def e2e_step():
+        xd = x_pin.to(dev, non_blocking=True)
+        qd = q_pin.to(dev, non_blocking=True)
+        debd = emp_sd_kde_fit_transform(xd, h, device=dev)
+        dd = kde_eval(debd, qd, h, device=dev)
+        out_pin.copy_(dd, non_blocking=True)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        dist.barrier()
+    for s_ev, e_ev in e2e_evs:
+        flush.zero_()
+        s_ev.record(stream)
+        e2e_step()
+        e_ev.record(stream)
+    torch.cuda.synchronize(dev)
+    e2e_ms = float(sum(s.elapsed_time(e) for s, e in e2e_evs))
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = world * pairs_step * args.steps / (e2e_ms * 1e-3)
+
+    # ---- accuracy spot check against FP64 ------------------------------------------
+    sub = slice(0, 128)
+    deb_np = deb.cpu().numpy()
+    dens_np = dens.cpu().numpy().astype(np.float64)
+    ref_logp = fp64.log_density(deb_np, q_np[sub], h)
+    kde_rel = np.abs(dens_np[sub] - np.exp(ref_logp)) / np.exp(ref_logp)
+    # debias of the first 64 rows against an FP64 score over the whole set
+    xs = x_np.astype(np.float64)
+    d2 = ((xs[:64, None, :] - xs[None, :, :]) ** 2).sum(-1)
+    phi = np.exp(-d2 / (2 * h * h))
+    deb64 = xs[:64] + 0.5 * ((phi @ xs) / (phi.sum(1, keepdims=True) + EPS) - xs[:64])
+    deb_abs = float(np.abs(deb_np[:64] - deb64).max())
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            cpu = cpu_baseline(12.0)
+        except Exception as exc:  # reported, not fatal
+            cpu = {"error": str(exc)[-300:]}
+
+    if rank == 0:
+        line = {
+            "metric": metric_name(),
+            "value": value,
+            "unit": "pair-evals/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32",
+            "data": "synthetic (seeded 8-component Gaussian mixture)",
+            "config": workload_config(),
+            "e2e": {"value": e2e_value, "unit": "pair-evals/s",
+                    "h2d_bytes_per_step": int(x_np.nbytes + q_np.nbytes), "d2h_bytes_per_step": int(N_QUERY * 4),
+                    "ms_per_step": e2e_ms / args.steps,
+                    "api": "flash_sd_kde.emp_sd_kde_fit_transform + flash_sd_kde.kde_eval"},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "sfu", "kernel": dom, "achieved": achieved, "peak": peak["peak"],
+                         "unit": "pair-evals/s (one exp per pair)",
+                         "frac": (achieved / peak["peak"]) if achieved else None,
+                         "traffic": traffic,
+                         "peak_source": "measured on this GPU: ex2.approx %.3e/s, fma.f32 %.3e/s "
+                                        "(fsk_diag_pipe_rates); P = R_sfu/(1-f*), c=%g, k=%g"
+                                        % (peak["r_sfu"], peak["r_fma"], C_OPS_PER_PAIR, K_OPS_PER_POLY_EXP),
+                         "sfu_only_peak": peak["r_sfu"]},
+            "kernels": kernels,
+            "cpu_baseline": cpu,
+            "clocks": sampler.summary(),
+            "accuracy": {"kde_max_rel_vs_fp64": float(kde_rel.max()), "kde_queries_checked": 128,
+                         "debias_max_abs_vs_fp64": deb_abs, "debias_rows_checked": 64},
+            "step_ms": step_ms,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,306 @@
+// fsk_api.cu - the extern "C" boundary (include/fsk.h).  Validates arguments,
+// sizes and carves the caller's workspace, and enqueues the kernels on the
+// caller's stream.  No allocation, no synchronisation (except
+// fsk_device_status), no host fallback.
+#include <math.h>
+
+#include <atomic>
+
+#include "fsk_kernels.cuh"
+#include "fsk_tc.cuh"
+
+namespace fsk {
+
+__device__ unsigned int g_device_error = 0u;
+
+static std::atomic<int64_t> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+int sm_count() {
+  int dev = 0, v = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 148;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) return 148;
+  return v;
+}
+
+int check_device() {
+  int dev = 0, major = 0, minor = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return FSK_ERR_CUDA;
+  if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess) return FSK_ERR_CUDA;
+  if (cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev) != cudaSuccess) return FSK_ERR_CUDA;
+  if (major != 10 || minor != 3) return FSK_ERR_UNSUPPORTED_DEVICE;
+  return FSK_OK;
+}
+
+int cuda_status(cudaError_t e) { return e == cudaSuccess ? FSK_OK : FSK_ERR_CUDA; }
+
+namespace {
+
+bool bad_bw(double h) { return !(h > 0.0) || !isfinite(h); }
+
+// ---- 16-D KDE workspace plan ---------------------------------------------------
+struct Kde16Plan {
+  bool ieee, atomic;
+  int simt_splits;
+  tc::TcPlan tcp;
+};
+
+Kde16Plan plan16(int64_t m, int64_t n, int flags) {
+  Kde16Plan p{};
+  p.ieee = (flags & FSK_PREC_IEEE) != 0;
+  p.atomic = (flags & FSK_ATOMIC) != 0;
+  if (p.ieee) p.simt_splits = simt_kde16_splits(m, n);
+  else p.tcp = tc::plan_kde16(m, n);
+  return p;
+}
+
+// common prefix: mean scratch, mu, mu64
+struct CenterBufs {
+  double* scratch;
+  float* mu;
+  double* mu64;
+};
+CenterBufs take_center(WsCarver& c, int64_t n) {
+  CenterBufs b;
+  b.scratch = c.take<double>(mean_scratch_doubles(n));
+  b.mu = c.take<float>(FSK_D);
+  b.mu64 = c.take<double>(FSK_D);
+  return b;
+}
+
+size_t kde16_bytes(int64_t m, int64_t n, const Kde16Plan& p) {
+  WsCarver c(nullptr, 0);
+  take_center(c, n);
+  if (p.ieee) {
+    c.take<double>((size_t)(p.atomic ? 1 : p.simt_splits) * m);
+  } else {
+    c.used = align_up(c.used, 256) + tc::tc_kde16_ws_bytes(p.tcp, m, p.atomic);
+  }
+  return align_up(c.used, 256);
+}
+
+constexpr int KNOWN_FLAGS = FSK_PREC_IEEE | FSK_LAPLACE | FSK_OUT_LOG | FSK_ATOMIC | FSK_WEIGHTED_FEATURE_MAJOR;
+
+}  // namespace
+}  // namespace fsk
+
+using namespace fsk;
+
+extern "C" {
+
+int fsk_version(void) { return 10000; }
+
+int64_t fsk_launch_count(void) { return g_launches.load(); }
+
+const char* fsk_strerror(int status) {
+  switch (status) {
+    case FSK_OK: return "ok";
+    case FSK_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case FSK_ERR_WORKSPACE_TOO_SMALL: return "workspace too small";
+    case FSK_ERR_CUDA: return "CUDA runtime error";
+    case FSK_ERR_DEVICE_TIMEOUT: return "bounded device wait timed out";
+    case FSK_ERR_UNSUPPORTED_DEVICE: return "device is not sm_103 (GB300)";
+    case FSK_ERR_SCRATCH_LIMIT: return "request exceeds the fixed scratch limit";
+    default: return "unknown status";
+  }
+}
+
+int fsk_device_status(void* stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return FSK_ERR_CUDA;
+  unsigned int v = 0, zero = 0;
+  e = cudaMemcpyFromSymbol(&v, g_device_error, sizeof(v));
+  if (e != cudaSuccess) return FSK_ERR_CUDA;
+  if (v != 0u) {
+    cudaMemcpyToSymbol(g_device_error, &zero, sizeof(zero));
+    return (int)(v & 0xFFu);
+  }
+  return FSK_OK;
+}
+
+size_t fsk_kde16_workspace_bytes(int64_t m, int64_t n, int flags) {
+  if (m < 1 || n < 1) return 0;
+  return kde16_bytes(m, n, plan16(m, n, flags));
+}
+
+int fsk_kde16(const float* queries, int64_t m, const float* data, int64_t n, double bandwidth, int flags,
+              double out_scale, double out_eps, float* out, void* workspace, size_t workspace_bytes,
+              void* stream) {
+  if (!queries || !data || !out || m < 1 || n < 1 || bad_bw(bandwidth)) return FSK_ERR_INVALID_ARGUMENT;
+  if (flags & ~KNOWN_FLAGS) return FSK_ERR_INVALID_ARGUMENT;
+  int st = check_device();
+  if (st) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const Kde16Plan p = plan16(m, n, flags);
+  if (!workspace || workspace_bytes < kde16_bytes(m, n, p)) return FSK_ERR_WORKSPACE_TOO_SMALL;
+  WsCarver c(workspace, workspace_bytes);
+  CenterBufs cb = take_center(c, n);
+  const bool laplace = (flags & FSK_LAPLACE) != 0;
+  double* part = nullptr;
+  int splits = 1;
+  if (p.ieee) {
+    splits = p.atomic ? 1 : p.simt_splits;
+    part = c.take<double>((size_t)splits * m);
+    if (!c.fits()) return FSK_ERR_WORKSPACE_TOO_SMALL;
+    if (p.atomic) launch_zero(part, m, s);
+    launch_kde16_simt(queries, m, data, n, bandwidth, laplace, p.simt_splits,
+                      p.atomic ? nullptr : part, p.atomic ? part : nullptr, s);
+  } else {
+    launch_mean16(data, n, cb.scratch, cb.mu, cb.mu64, s);
+    st = tc::launch_kde16_tc(queries, m, data, n, cb.mu, bandwidth, laplace, p.tcp, c, &part, p.atomic, s);
+    if (st) return st;
+    splits = p.atomic ? 1 : (int)p.tcp.splits;
+  }
+  launch_reduce_rows(part, splits, m, out_scale, out_eps, (flags & FSK_OUT_LOG) != 0, out, s);
+  return cuda_status(cudaGetLastError());
+}
+
+// ---- empirical score ------------------------------------------------------------
+static size_t empscore_bytes(int64_t n, int variant, int splits) {
+  WsCarver c(nullptr, 0);
+  take_center(c, n);
+  if (variant == FSK_SCORE_SYMMETRIC) {
+    c.take<double>((size_t)n);
+    c.take<double>((size_t)n * FSK_D);
+  } else {
+    c.take<double>((size_t)splits * n);
+    c.take<double>((size_t)splits * n * FSK_D);
+  }
+  return align_up(c.used, 256);
+}
+
+size_t fsk_empscore16_workspace_bytes(int64_t n, int variant, int flags) {
+  (void)flags;
+  if (n < 1) return 0;
+  return empscore_bytes(n, variant, simt_score16_splits(n));
+}
+
+int fsk_empscore16(const float* data, int64_t n, double bandwidth, int variant, int flags, float* pdf_sum,
+                   float* weighted_sum, void* workspace, size_t workspace_bytes, void* stream) {
+  if (!data || !pdf_sum || !weighted_sum || n < 1 || bad_bw(bandwidth)) return FSK_ERR_INVALID_ARGUMENT;
+  if (variant != FSK_SCORE_ORDERED && variant != FSK_SCORE_SYMMETRIC) return FSK_ERR_INVALID_ARGUMENT;
+  if (flags & ~KNOWN_FLAGS) return FSK_ERR_INVALID_ARGUMENT;
+  int st = check_device();
+  if (st) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int splits = simt_score16_splits(n);
+  if (!workspace || workspace_bytes < empscore_bytes(n, variant, splits)) return FSK_ERR_WORKSPACE_TOO_SMALL;
+  WsCarver c(workspace, workspace_bytes);
+  CenterBufs cb = take_center(c, n);
+  launch_mean16(data, n, cb.scratch, cb.mu, cb.mu64, s);
+  const bool fm = (flags & FSK_WEIGHTED_FEATURE_MAJOR) != 0;
+  const int64_t ws_row = fm ? 1 : FSK_D, ws_col = fm ? n : 1;
+  if (variant == FSK_SCORE_SYMMETRIC) {
+    double* apdf = c.take<double>((size_t)n);
+    double* aw = c.take<double>((size_t)n * FSK_D);
+    launch_zero(apdf, n, s);
+    launch_zero(aw, n * FSK_D, s);
+    launch_score16_sym_simt(data, n, cb.mu, bandwidth, apdf, aw, s);
+    launch_reduce_score(apdf, aw, 1, n, cb.mu64, pdf_sum, weighted_sum, ws_row, ws_col, s);
+  } else {
+    double* ppdf = c.take<double>((size_t)splits * n);
+    double* pw = c.take<double>((size_t)splits * n * FSK_D);
+    launch_score16_simt(data, n, cb.mu, bandwidth, splits, ppdf, pw, s);
+    launch_reduce_score(ppdf, pw, splits, n, cb.mu64, pdf_sum, weighted_sum, ws_row, ws_col, s);
+  }
+  return cuda_status(cudaGetLastError());
+}
+
+int fsk_debias16(const float* data, int64_t n, const float* pdf_sum, const float* weighted_sum,
+                 int64_t w_row_stride, int64_t w_col_stride, double bandwidth, double eps, float* debiased,
+                 float* score, void* stream) {
+  if (!data || !pdf_sum || !weighted_sum || !debiased || n < 1 || bad_bw(bandwidth) || !(eps >= 0.0))
+    return FSK_ERR_INVALID_ARGUMENT;
+  int st = check_device();
+  if (st) return st;
+  launch_debias16(data, n, pdf_sum, weighted_sum, w_row_stride, w_col_stride, bandwidth, eps, debiased,
+                  score, static_cast<cudaStream_t>(stream));
+  return cuda_status(cudaGetLastError());
+}
+
+// ---- 1-D ------------------------------------------------------------------------
+size_t fsk_kde1d_workspace_bytes(int64_t m, int64_t n, int flags) {
+  if (m < 1 || n < 1) return 0;
+  const int splits = (flags & FSK_ATOMIC) ? 1 : kde1d_splits(m, n);
+  // the score variant needs two partial arrays
+  return align_up((size_t)2 * splits * m * sizeof(double), 256);
+}
+
+int fsk_kde1d(const float* queries, int64_t m, const float* data, int64_t n, double bandwidth, int flags,
+              double out_scale, double out_eps, float* out, void* workspace, size_t workspace_bytes,
+              void* stream) {
+  if (!queries || !data || !out || m < 1 || n < 1 || bad_bw(bandwidth)) return FSK_ERR_INVALID_ARGUMENT;
+  if (flags & ~KNOWN_FLAGS) return FSK_ERR_INVALID_ARGUMENT;
+  int st = check_device();
+  if (st) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!workspace || workspace_bytes < fsk_kde1d_workspace_bytes(m, n, flags)) return FSK_ERR_WORKSPACE_TOO_SMALL;
+  const bool atomic = (flags & FSK_ATOMIC) != 0;
+  const int splits = kde1d_splits(m, n);
+  double* part = static_cast<double*>(workspace);
+  if (atomic) launch_zero(part, m, s);
+  launch_kde1d(queries, m, data, n, bandwidth, (flags & FSK_LAPLACE) != 0, splits, atomic ? nullptr : part,
+               atomic ? part : nullptr, s);
+  launch_reduce_rows(part, atomic ? 1 : splits, m, out_scale, out_eps, (flags & FSK_OUT_LOG) != 0, out, s);
+  return cuda_status(cudaGetLastError());
+}
+
+int fsk_kde1d_score(const float* queries, int64_t m, const float* data, int64_t n, double bandwidth,
+                    float* score, float* pdf, float* deriv, void* workspace, size_t workspace_bytes,
+                    void* stream) {
+  if (!queries || !data || m < 1 || n < 1 || bad_bw(bandwidth)) return FSK_ERR_INVALID_ARGUMENT;
+  int st = check_device();
+  if (st) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!workspace || workspace_bytes < fsk_kde1d_workspace_bytes(m, n, 0)) return FSK_ERR_WORKSPACE_TOO_SMALL;
+  const int splits = kde1d_splits(m, n);
+  double* p0 = static_cast<double*>(workspace);
+  double* p1 = p0 + (size_t)splits * m;
+  launch_kde1d_score(queries, m, data, n, bandwidth, splits, p0, p1, s);
+  launch_reduce_kde1d_score(p0, p1, splits, m, n, bandwidth, score, pdf, deriv, s);
+  return cuda_status(cudaGetLastError());
+}
+
+// ---- bandwidth --------------------------------------------------------------------
+size_t fsk_silverman_workspace_bytes(int64_t n, int d) {
+  if (n < 1 || d < 1) return 0;
+  return silverman_ws_bytes(n, d);
+}
+
+int fsk_silverman(const float* data, int64_t n, int d, int rule, double* h_out, void* workspace,
+                  size_t workspace_bytes, void* stream) {
+  if (!data || !h_out || n < 1 || d < 1 || d > 64) return FSK_ERR_INVALID_ARGUMENT;
+  if (rule != FSK_RULE_SILVERMAN && rule != FSK_RULE_SDKDE_1D) return FSK_ERR_INVALID_ARGUMENT;
+  if (rule == FSK_RULE_SDKDE_1D && d != 1) return FSK_ERR_INVALID_ARGUMENT;
+  int st = check_device();
+  if (st) return st;
+  if (!workspace || workspace_bytes < silverman_ws_bytes(n, d)) return FSK_ERR_WORKSPACE_TOO_SMALL;
+  return run_silverman(data, n, d, rule, h_out, workspace, workspace_bytes, static_cast<cudaStream_t>(stream));
+}
+
+int fsk_reduce_partials(const float* partials, int64_t splits, int64_t count, float* out, void* stream) {
+  if (!partials || !out || splits < 1 || count < 0) return FSK_ERR_INVALID_ARGUMENT;
+  if (count == 0) return FSK_OK;
+  int st = check_device();
+  if (st) return st;
+  launch_reduce_f32_partials(partials, splits, count, out, static_cast<cudaStream_t>(stream));
+  return cuda_status(cudaGetLastError());
+}
+
+// ---- diagnostics: single-MMA probe (not part of fsk.h's hot path) ----------------
+int fsk_diag_wait_timeout_probe(int* out, void* stream) {
+  if (!out) return FSK_ERR_INVALID_ARGUMENT;
+  int st = check_device();
+  if (st) return st;
+  return tc::launch_wait_timeout_probe(out, static_cast<cudaStream_t>(stream));
+}
+
+int fsk_diag_mma_probe(const float* a, const float* b, float* d, void* stream) {
+  if (!a || !b || !d) return FSK_ERR_INVALID_ARGUMENT;
+  int st = check_device();
+  if (st) return st;
+  return tc::launch_mma_probe(a, b, d, static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,491 @@
+// fsk_simt.cu - CUDA-core kernels of the Flash-SD-KDE hot path.
+//
+// * 16-D KDE and empirical score in the "fp32_ieee" precision mode: every
+//   pair distance is formed from direct FP32 differences sum_k (q_k - x_k)^2
+//   (no cancellation), exp on the SFU (ex2.approx), and per-split compensated
+//   FP32 sums written as FP64 partials [split][row].  Follows the math of
+//   flash_sd_kde/reference.py:216-235 (KDE) and :263-284 (score); the split-K
+//   decomposition follows kernels/kde_eval_16d_stream_splitk.py:14-81 and
+//   kernels/emp_score_16d_ordered_splitk.py:14-92.
+// * Symmetric score (phi_ij = phi_ji): upper-triangle tile pairs, row and
+//   column contributions scattered with FP64 atomics, after
+//   kernels/emp_score_16d_symmetric_atomic.py:10-103.
+// * 1-D KDE and 1-D KDE score (pdf + derivative sums), after
+//   kernels/kde_eval_1d_splitk.py:13-52 and kernels/flash_sd_kde/kde.py:59-100.
+//
+// Distances come from direct FP32 differences of the original coordinates
+// (four FMA chains joined pairwise) and the exponent product dist * log2(e)/(2h^2)
+// is carried in double-float (exp2_neg_scaled), so no step needs centring.
+#include "fsk_common.cuh"
+#include "fsk_kernels.cuh"
+
+namespace fsk {
+
+// ---------------------------------------------------------------------------
+// 16-D KDE, direct differences.  Block: 128 threads x QPT queries each.
+// grid.x = query blocks, grid.y = splits; each split covers `tiles_per_split`
+// data tiles of TN points.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int SIMT_TN = 64;
+constexpr int SIMT_THREADS = 128;
+constexpr int SIMT_QPT = 2;
+}  // namespace
+
+template <bool LAPLACE>
+__global__ void __launch_bounds__(SIMT_THREADS) kde16_simt_kernel(
+    const float* __restrict__ q, int64_t m, const float* __restrict__ x, int64_t n,
+    float c2, float c2_lo, float c1, int64_t tiles_per_split,
+    double* __restrict__ partials, double* __restrict__ atomic_acc) {
+  __shared__ __align__(16) float xs[SIMT_TN][FSK_D];
+
+  const int64_t q0 = (int64_t)blockIdx.x * (SIMT_THREADS * SIMT_QPT);
+  float qr[SIMT_QPT][FSK_D];
+  bool qvalid[SIMT_QPT];
+#pragma unroll
+  for (int u = 0; u < SIMT_QPT; ++u) {
+    int64_t qi = q0 + threadIdx.x + u * SIMT_THREADS;
+    qvalid[u] = qi < m;
+#pragma unroll
+    for (int k = 0; k < FSK_D; ++k) qr[u][k] = qvalid[u] ? q[qi * FSK_D + k] : 0.f;
+  }
+  Comp acc[SIMT_QPT];
+#pragma unroll
+  for (int u = 0; u < SIMT_QPT; ++u) acc[u] = Comp{0.f, 0.f};
+
+  const int64_t n_tiles = (n + SIMT_TN - 1) / SIMT_TN;
+  const int64_t t_begin = (int64_t)blockIdx.y * tiles_per_split;
+  const int64_t t_end = min(n_tiles, t_begin + tiles_per_split);
+  for (int64_t t = t_begin; t < t_end; ++t) {
+    const int64_t j0 = t * SIMT_TN;
+    const int valid = (int)imin<int64_t>(SIMT_TN, n - j0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < SIMT_TN * FSK_D; e += SIMT_THREADS) {
+      int r = e / FSK_D, k = e % FSK_D;
+      xs[r][k] = r < valid ? x[(j0 + r) * FSK_D + k] : 0.f;
+    }
+    __syncthreads();
+    float part[SIMT_QPT];
+#pragma unroll
+    for (int u = 0; u < SIMT_QPT; ++u) part[u] = 0.f;
+    for (int r = 0; r < valid; ++r) {
+      float xv[FSK_D];
+#pragma unroll
+      for (int k = 0; k < FSK_D; k += 4) {
+        float4 v = *reinterpret_cast<const float4*>(&xs[r][k]);
+        xv[k] = v.x; xv[k + 1] = v.y; xv[k + 2] = v.z; xv[k + 3] = v.w;
+      }
+#pragma unroll
+      for (int u = 0; u < SIMT_QPT; ++u) {
+        const float dist = sqdist16(qr[u], xv);
+        float e = exp2_neg_scaled(dist, c2, c2_lo);
+        if (LAPLACE) e *= fmaf(-c1, dist, 1.0f + 0.5f * FSK_D);
+        part[u] += e;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < SIMT_QPT; ++u) acc[u].add(part[u]);
+  }
+#pragma unroll
+  for (int u = 0; u < SIMT_QPT; ++u) {
+    int64_t qi = q0 + threadIdx.x + u * SIMT_THREADS;
+    if (!qvalid[u]) continue;
+    double v = (double)acc[u].s + (double)acc[u].c;
+    if (atomic_acc) atomicAdd(&atomic_acc[qi], v);
+    else partials[(int64_t)blockIdx.y * m + qi] = v;
+  }
+}
+
+void launch_kde16_simt(const float* q, int64_t m, const float* x, int64_t n, double h, bool laplace,
+                       int splits, double* partials, double* atomic_acc, cudaStream_t s) {
+  const int64_t n_tiles = (n + SIMT_TN - 1) / SIMT_TN;
+  const int64_t tps = (n_tiles + splits - 1) / splits;
+  const int qblocks = (int)((m + SIMT_THREADS * SIMT_QPT - 1) / (SIMT_THREADS * SIMT_QPT));
+  dim3 grid(qblocks, (unsigned)((n_tiles + tps - 1) / tps));
+  const double c2d = FSK_LOG2E / (2.0 * h * h);
+  const float c2 = (float)c2d, c2_lo = (float)(c2d - (double)c2);
+  const float c1 = (float)(1.0 / (2.0 * h * h));
+  TimerScope ts(K_KDE16_SIMT, (double)m * (double)n, s);
+  if (laplace)
+    kde16_simt_kernel<true><<<grid, SIMT_THREADS, 0, s>>>(q, m, x, n, c2, c2_lo, c1, tps, partials, atomic_acc);
+  else
+    kde16_simt_kernel<false><<<grid, SIMT_THREADS, 0, s>>>(q, m, x, n, c2, c2_lo, c1, tps, partials, atomic_acc);
+  count_launch();
+}
+
+// Effective split count: the launchers give each split ceil(n_tiles/splits)
+// tiles, so the number of non-empty splits is ceil(n_tiles / tps); the
+// partial buffers and reductions use exactly this count.
+static int effective_splits(int64_t n_tiles, int64_t splits) {
+  splits = imax<int64_t>(1, imin<int64_t>(splits, n_tiles));
+  const int64_t tps = (n_tiles + splits - 1) / splits;
+  return (int)((n_tiles + tps - 1) / tps);
+}
+
+int simt_kde16_splits(int64_t m, int64_t n) {
+  const int64_t n_tiles = (n + SIMT_TN - 1) / SIMT_TN;
+  const int64_t qblocks = (m + SIMT_THREADS * SIMT_QPT - 1) / (SIMT_THREADS * SIMT_QPT);
+  const int64_t target = 4LL * sm_count() * 4;  // ~4 waves of 4 resident blocks/SM
+  int64_t splits = (target + qblocks - 1) / qblocks;
+  splits = imax<int64_t>(1, imin<int64_t>(splits, n_tiles / 4 > 0 ? n_tiles / 4 : 1));
+  return effective_splits(n_tiles, imin<int64_t>(splits, 65535));
+}
+
+// ---------------------------------------------------------------------------
+// 16-D empirical score, ordered split-K.  One row i per thread.  Writes
+// partial pdf [split][n] and partial weighted [split][n][16].  Distances use
+// the original coordinates; the weighted sums accumulate x_j - mu (centred,
+// so the compensated FP32 sums carry the spread, not the offset) and the
+// mean is added back in FP64 by the reduction.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(SIMT_THREADS) score16_simt_kernel(
+    const float* __restrict__ x, int64_t n, const float* __restrict__ mu, float c2, float c2_lo,
+    int64_t tiles_per_split, double* __restrict__ ppdf, double* __restrict__ pw) {
+  __shared__ __align__(16) float xs[SIMT_TN][FSK_D];
+  __shared__ __align__(16) float xcs[SIMT_TN][FSK_D];
+  __shared__ float mus[FSK_D];
+  if (threadIdx.x < FSK_D) mus[threadIdx.x] = mu[threadIdx.x];
+  __syncthreads();
+  const int64_t i = (int64_t)blockIdx.x * SIMT_THREADS + threadIdx.x;
+  const bool valid_i = i < n;
+  float xi[FSK_D];
+#pragma unroll
+  for (int k = 0; k < FSK_D; ++k) xi[k] = valid_i ? x[i * FSK_D + k] : 0.f;
+  Comp pdf{0.f, 0.f};
+  Comp w[FSK_D];
+#pragma unroll
+  for (int k = 0; k < FSK_D; ++k) w[k] = Comp{0.f, 0.f};
+
+  const int64_t n_tiles = (n + SIMT_TN - 1) / SIMT_TN;
+  const int64_t t_begin = (int64_t)blockIdx.y * tiles_per_split;
+  const int64_t t_end = min(n_tiles, t_begin + tiles_per_split);
+  for (int64_t t = t_begin; t < t_end; ++t) {
+    const int64_t j0 = t * SIMT_TN;
+    const int valid = (int)imin<int64_t>(SIMT_TN, n - j0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < SIMT_TN * FSK_D; e += SIMT_THREADS) {
+      int r = e / FSK_D, k = e % FSK_D;
+      const float v = r < valid ? x[(j0 + r) * FSK_D + k] : 0.f;
+      xs[r][k] = v;
+      xcs[r][k] = r < valid ? v - mus[k] : 0.f;
+    }
+    __syncthreads();
+    float ps = 0.f;
+    float wp[FSK_D];
+#pragma unroll
+    for (int k = 0; k < FSK_D; ++k) wp[k] = 0.f;
+    for (int r = 0; r < valid; ++r) {
+      float xv[FSK_D], xc[FSK_D];
+#pragma unroll
+      for (int k = 0; k < FSK_D; k += 4) {
+        float4 v = *reinterpret_cast<const float4*>(&xs[r][k]);
+        xv[k] = v.x; xv[k + 1] = v.y; xv[k + 2] = v.z; xv[k + 3] = v.w;
+        float4 c = *reinterpret_cast<const float4*>(&xcs[r][k]);
+        xc[k] = c.x; xc[k + 1] = c.y; xc[k + 2] = c.z; xc[k + 3] = c.w;
+      }
+      const float e = exp2_neg_scaled(sqdist16(xi, xv), c2, c2_lo);
+      ps += e;
+#pragma unroll
+      for (int k = 0; k < FSK_D; ++k) wp[k] = fmaf(e, xc[k], wp[k]);
+    }
+    pdf.add(ps);
+#pragma unroll
+    for (int k = 0; k < FSK_D; ++k) w[k].add(wp[k]);
+  }
+  if (!valid_i) return;
+  ppdf[(int64_t)blockIdx.y * n + i] = (double)pdf.s + (double)pdf.c;
+  double* wo = pw + ((int64_t)blockIdx.y * n + i) * FSK_D;
+#pragma unroll
+  for (int k = 0; k < FSK_D; ++k) wo[k] = (double)w[k].s + (double)w[k].c;
+}
+
+void launch_score16_simt(const float* x, int64_t n, const float* mu, double h, int splits,
+                         double* ppdf, double* pw, cudaStream_t s) {
+  const int64_t n_tiles = (n + SIMT_TN - 1) / SIMT_TN;
+  const int64_t tps = (n_tiles + splits - 1) / splits;
+  dim3 grid((unsigned)((n + SIMT_THREADS - 1) / SIMT_THREADS), (unsigned)((n_tiles + tps - 1) / tps));
+  const double c2d = FSK_LOG2E / (2.0 * h * h);
+  const float c2 = (float)c2d, c2_lo = (float)(c2d - (double)c2);
+  TimerScope ts(K_SCORE16_SIMT, (double)n * (double)n, s);
+  score16_simt_kernel<<<grid, SIMT_THREADS, 0, s>>>(x, n, mu, c2, c2_lo, tps, ppdf, pw);
+  count_launch();
+}
+
+int simt_score16_splits(int64_t n) {
+  const int64_t n_tiles = (n + SIMT_TN - 1) / SIMT_TN;
+  const int64_t rblocks = (n + SIMT_THREADS - 1) / SIMT_THREADS;
+  const int64_t target = 4LL * sm_count() * 4;
+  int64_t splits = (target + rblocks - 1) / rblocks;
+  splits = imax<int64_t>(1, imin<int64_t>(splits, n_tiles / 4 > 0 ? n_tiles / 4 : 1));
+  return effective_splits(n_tiles, imin<int64_t>(splits, 65535));
+}
+
+// ---------------------------------------------------------------------------
+// 16-D empirical score, symmetric.  One block per upper-triangle tile pair
+// (I <= J) of SYM_T rows; thread t owns row I*SYM_T + t.  Row sums are kept
+// in registers; column sums go through warp shuffles and shared FP32 into
+// FP64 atomics on the accumulators acc_pdf[n], acc_w[n][16].
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int SYM_T = 64;
+}
+
+__global__ void __launch_bounds__(SYM_T) score16_sym_simt_kernel(
+    const float* __restrict__ x, int64_t n, const float* __restrict__ mu, float c2, float c2_lo,
+    int64_t n_tiles, double* __restrict__ acc_pdf, double* __restrict__ acc_w) {
+  // Map the linear block id to an upper-triangle pair (I, J), I <= J.
+  const int64_t b = blockIdx.x;
+  // row I has (n_tiles - I) pairs; find I by walking (n_tiles is moderate).
+  int64_t I = 0, rem = b;
+  {
+    // closed form start: solve I from cumulative counts.
+    double nt = (double)n_tiles;
+    double disc = (2.0 * nt + 1.0) * (2.0 * nt + 1.0) - 8.0 * (double)b;
+    int64_t guess = (int64_t)floor(((2.0 * nt + 1.0) - sqrt(fmax(disc, 0.0))) / 2.0);
+    guess = imax<int64_t>(0, imin<int64_t>(guess, n_tiles - 1));
+    auto start = [&](int64_t r) { return r * n_tiles - r * (r - 1) / 2; };
+    while (guess > 0 && start(guess) > b) --guess;
+    while (guess + 1 < n_tiles && start(guess + 1) <= b) ++guess;
+    I = guess;
+    rem = b - start(I);
+  }
+  const int64_t J = I + rem;
+
+  __shared__ __align__(16) float xj[SYM_T][FSK_D];
+  __shared__ float col_acc[SYM_T][FSK_D + 1];
+  __shared__ float mus[FSK_D];
+  if (threadIdx.x < FSK_D) mus[threadIdx.x] = mu[threadIdx.x];
+  __syncthreads();
+  const int64_t i = I * SYM_T + threadIdx.x;
+  const bool vi = i < n;
+  float xi[FSK_D], xic[FSK_D];
+#pragma unroll
+  for (int k = 0; k < FSK_D; ++k) {
+    xi[k] = vi ? x[i * FSK_D + k] : 0.f;
+    xic[k] = vi ? xi[k] - mus[k] : 0.f;
+  }
+  const int64_t j0 = J * SYM_T;
+  const int validj = (int)imin<int64_t>(SYM_T, n - j0);
+  for (int e = threadIdx.x; e < SYM_T * FSK_D; e += SYM_T) {
+    int r = e / FSK_D, k = e % FSK_D;
+    xj[r][k] = r < validj ? x[(j0 + r) * FSK_D + k] : 0.f;
+  }
+  for (int e = threadIdx.x; e < SYM_T * (FSK_D + 1); e += SYM_T) (&col_acc[0][0])[e] = 0.f;
+  __syncthreads();
+
+  const bool diag = (I == J);
+  float prow = 0.f, wrow[FSK_D];
+#pragma unroll
+  for (int k = 0; k < FSK_D; ++k) wrow[k] = 0.f;
+  for (int r = 0; r < validj; ++r) {
+    float xv[FSK_D];
+#pragma unroll
+    for (int k = 0; k < FSK_D; k += 4) {
+      float4 v = *reinterpret_cast<const float4*>(&xj[r][k]);
+      xv[k] = v.x; xv[k + 1] = v.y; xv[k + 2] = v.z; xv[k + 3] = v.w;
+    }
+    const float e = exp2_neg_scaled(sqdist16(xi, xv), c2, c2_lo);
+    // row contribution: all (i, j) in the tile pair; on the diagonal tile only j >= i
+    float er = (vi && (!diag || r >= (int)threadIdx.x)) ? e : 0.f;
+    prow += er;
+#pragma unroll
+    for (int k = 0; k < FSK_D; ++k) wrow[k] = fmaf(er, xv[k] - mus[k], wrow[k]);
+    // column contribution (j receives phi_ij * x_i): off-diagonal pairs, or j > i on the diagonal
+    float ec = (vi && (!diag || r > (int)threadIdx.x)) ? e : 0.f;
+    float cv[FSK_D + 1];
+    cv[FSK_D] = ec;
+#pragma unroll
+    for (int k = 0; k < FSK_D; ++k) cv[k] = ec * xic[k];
+#pragma unroll
+    for (int k = 0; k <= FSK_D; ++k) {
+      float v = cv[k];
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+      cv[k] = v;
+    }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+      for (int k = 0; k <= FSK_D; ++k) atomicAdd(&col_acc[r][k], cv[k]);
+    }
+  }
+  __syncthreads();
+  if (vi) {
+    atomicAdd(&acc_pdf[i], (double)prow);
+#pragma unroll
+    for (int k = 0; k < FSK_D; ++k) atomicAdd(&acc_w[i * FSK_D + k], (double)wrow[k]);
+  }
+  if (threadIdx.x < validj) {
+    const int64_t j = j0 + threadIdx.x;
+    atomicAdd(&acc_pdf[j], (double)col_acc[threadIdx.x][FSK_D]);
+#pragma unroll
+    for (int k = 0; k < FSK_D; ++k) atomicAdd(&acc_w[j * FSK_D + k], (double)col_acc[threadIdx.x][k]);
+  }
+}
+
+void launch_score16_sym_simt(const float* x, int64_t n, const float* mu, double h, double* acc_pdf,
+                             double* acc_w, cudaStream_t s) {
+  const int64_t n_tiles = (n + SYM_T - 1) / SYM_T;
+  const int64_t pairs = n_tiles * (n_tiles + 1) / 2;
+  const double c2d = FSK_LOG2E / (2.0 * h * h);
+  const float c2 = (float)c2d, c2_lo = (float)(c2d - (double)c2);
+  TimerScope ts(K_SCORE16_SYM_SIMT, 0.5 * (double)n * (double)(n + 1), s);
+  score16_sym_simt_kernel<<<(unsigned)pairs, SYM_T, 0, s>>>(x, n, mu, c2, c2_lo, n_tiles, acc_pdf, acc_w);
+  count_launch();
+}
+
+int64_t sym_simt_pairs(int64_t n) {
+  const int64_t n_tiles = (n + SYM_T - 1) / SYM_T;
+  return n_tiles * (n_tiles + 1) / 2;
+}
+
+// ---------------------------------------------------------------------------
+// 1-D KDE.  Block 128 threads x Q1 queries; data tiles of T1 points in SMEM.
+// phi = exp(-(q - x)^2 / (2 h^2)) (times 1.5 - (q-x)^2/(2h^2) with Laplace).
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int K1_THREADS = 128;
+constexpr int K1_Q = 8;
+constexpr int K1_T = 1024;
+}  // namespace
+
+template <bool LAPLACE>
+__global__ void __launch_bounds__(K1_THREADS) kde1d_kernel(
+    const float* __restrict__ q, int64_t m, const float* __restrict__ x, int64_t n, float nc2,
+    float c1, int64_t tiles_per_split, double* __restrict__ partials, double* __restrict__ atomic_acc) {
+  __shared__ __align__(16) float xs[K1_T];
+  const int64_t q0 = (int64_t)blockIdx.x * (K1_THREADS * K1_Q);
+  float qr[K1_Q];
+#pragma unroll
+  for (int u = 0; u < K1_Q; ++u) {
+    int64_t qi = q0 + threadIdx.x + u * K1_THREADS;
+    qr[u] = qi < m ? q[qi] : 0.f;
+  }
+  Comp acc[K1_Q];
+#pragma unroll
+  for (int u = 0; u < K1_Q; ++u) acc[u] = Comp{0.f, 0.f};
+  const int64_t n_tiles = (n + K1_T - 1) / K1_T;
+  const int64_t t_begin = (int64_t)blockIdx.y * tiles_per_split;
+  const int64_t t_end = min(n_tiles, t_begin + tiles_per_split);
+  for (int64_t t = t_begin; t < t_end; ++t) {
+    const int64_t j0 = t * K1_T;
+    const int valid = (int)imin<int64_t>(K1_T, n - j0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < K1_T; e += K1_THREADS) xs[e] = e < valid ? x[j0 + e] : 0.f;
+    __syncthreads();
+    for (int r0 = 0; r0 < valid; r0 += 32) {
+      float part[K1_Q];
+#pragma unroll
+      for (int u = 0; u < K1_Q; ++u) part[u] = 0.f;
+      const int rend = min(valid, r0 + 32);
+      for (int r = r0; r < rend; ++r) {
+        const float xv = xs[r];
+#pragma unroll
+        for (int u = 0; u < K1_Q; ++u) {
+          float d = qr[u] - xv;
+          float t2 = d * d;
+          float e = ex2_approx(t2 * nc2);
+          if (LAPLACE) e *= fmaf(-c1, t2, 1.5f);
+          part[u] += e;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < K1_Q; ++u) acc[u].add(part[u]);
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < K1_Q; ++u) {
+    int64_t qi = q0 + threadIdx.x + u * K1_THREADS;
+    if (qi >= m) continue;
+    double v = (double)acc[u].s + (double)acc[u].c;
+    if (atomic_acc) atomicAdd(&atomic_acc[qi], v);
+    else partials[(int64_t)blockIdx.y * m + qi] = v;
+  }
+}
+
+int kde1d_splits(int64_t m, int64_t n) {
+  const int64_t n_tiles = (n + K1_T - 1) / K1_T;
+  const int64_t qblocks = (m + K1_THREADS * K1_Q - 1) / (K1_THREADS * K1_Q);
+  const int64_t target = 8LL * sm_count() * 4;
+  int64_t splits = (target + qblocks - 1) / qblocks;
+  return effective_splits(n_tiles, imin<int64_t>(splits, 65535));
+}
+
+void launch_kde1d(const float* q, int64_t m, const float* x, int64_t n, double h, bool laplace,
+                  int splits, double* partials, double* atomic_acc, cudaStream_t s) {
+  const int64_t n_tiles = (n + K1_T - 1) / K1_T;
+  const int64_t tps = (n_tiles + splits - 1) / splits;
+  dim3 grid((unsigned)((m + K1_THREADS * K1_Q - 1) / (K1_THREADS * K1_Q)), (unsigned)((n_tiles + tps - 1) / tps));
+  const float nc2 = (float)(-FSK_LOG2E / (2.0 * h * h));
+  const float c1 = (float)(1.0 / (2.0 * h * h));
+  TimerScope ts(K_KDE1D, (double)m * (double)n, s);
+  if (laplace)
+    kde1d_kernel<true><<<grid, K1_THREADS, 0, s>>>(q, m, x, n, nc2, c1, tps, partials, atomic_acc);
+  else
+    kde1d_kernel<false><<<grid, K1_THREADS, 0, s>>>(q, m, x, n, nc2, c1, tps, partials, atomic_acc);
+  count_launch();
+}
+
+// 1-D pdf + derivative sums: S0 = sum phi, S1 = sum (x - q) phi  (= -h * sum z phi).
+__global__ void __launch_bounds__(K1_THREADS) kde1d_score_kernel(
+    const float* __restrict__ q, int64_t m, const float* __restrict__ x, int64_t n, float nc2,
+    int64_t tiles_per_split, double* __restrict__ p0, double* __restrict__ p1) {
+  __shared__ __align__(16) float xs[K1_T];
+  const int64_t q0 = (int64_t)blockIdx.x * (K1_THREADS * K1_Q);
+  float qr[K1_Q];
+#pragma unroll
+  for (int u = 0; u < K1_Q; ++u) {
+    int64_t qi = q0 + threadIdx.x + u * K1_THREADS;
+    qr[u] = qi < m ? q[qi] : 0.f;
+  }
+  Comp a0[K1_Q], a1[K1_Q];
+#pragma unroll
+  for (int u = 0; u < K1_Q; ++u) { a0[u] = Comp{0.f, 0.f}; a1[u] = Comp{0.f, 0.f}; }
+  const int64_t n_tiles = (n + K1_T - 1) / K1_T;
+  const int64_t t_begin = (int64_t)blockIdx.y * tiles_per_split;
+  const int64_t t_end = min(n_tiles, t_begin + tiles_per_split);
+  for (int64_t t = t_begin; t < t_end; ++t) {
+    const int64_t j0 = t * K1_T;
+    const int valid = (int)imin<int64_t>(K1_T, n - j0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < K1_T; e += K1_THREADS) xs[e] = e < valid ? x[j0 + e] : 0.f;
+    __syncthreads();
+    for (int r0 = 0; r0 < valid; r0 += 32) {
+      float s0[K1_Q], s1[K1_Q];
+#pragma unroll
+      for (int u = 0; u < K1_Q; ++u) { s0[u] = 0.f; s1[u] = 0.f; }
+      const int rend = min(valid, r0 + 32);
+      for (int r = r0; r < rend; ++r) {
+        const float xv = xs[r];
+#pragma unroll
+        for (int u = 0; u < K1_Q; ++u) {
+          float d = qr[u] - xv;
+          float e = ex2_approx(d * d * nc2);
+          s0[u] += e;
+          s1[u] = fmaf(-d, e, s1[u]);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < K1_Q; ++u) { a0[u].add(s0[u]); a1[u].add(s1[u]); }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < K1_Q; ++u) {
+    int64_t qi = q0 + threadIdx.x + u * K1_THREADS;
+    if (qi >= m) continue;
+    p0[(int64_t)blockIdx.y * m + qi] = (double)a0[u].s + (double)a0[u].c;
+    p1[(int64_t)blockIdx.y * m + qi] = (double)a1[u].s + (double)a1[u].c;
+  }
+}
+
+void launch_kde1d_score(const float* q, int64_t m, const float* x, int64_t n, double h, int splits,
+                        double* p0, double* p1, cudaStream_t s) {
+  const int64_t n_tiles = (n + K1_T - 1) / K1_T;
+  const int64_t tps = (n_tiles + splits - 1) / splits;
+  dim3 grid((unsigned)((m + K1_THREADS * K1_Q - 1) / (K1_THREADS * K1_Q)), (unsigned)((n_tiles + tps - 1) / tps));
+  const float nc2 = (float)(-FSK_LOG2E / (2.0 * h * h));
+  TimerScope ts(K_KDE1D_SCORE, (double)m * (double)n, s);
+  kde1d_score_kernel<<<grid, K1_THREADS, 0, s>>>(q, m, x, n, nc2, tps, p0, p1);
+  count_launch();
+}
+
+}  // namespace fsk

@@ -1,0 +1,87 @@
+// fsk_tc.cuh - tile geometry, parameters and launchers of the tcgen05 kernels.
+#pragma once
+#include "fsk_common.cuh"
+
+namespace fsk {
+namespace tc {
+
+// ---- geometry -----------------------------------------------------------------
+constexpr int QT = 128;                 // queries per MMA tile (M, one TMEM lane each)
+constexpr int NQT = 4;                  // query tiles per work unit (512 queries)
+constexpr int NT = 64;                  // data points per stage (MMA N)
+constexpr int NS = 8;                   // shared-memory data stages
+constexpr int KH = 32;                  // K of the "hi" operand: 16 features + 16 bias columns
+// Operand images, fp16, no-swizzle K-major core-matrix layout: 8-row groups,
+// each group = (K/8) core matrices of 8 rows x 16 B stored back to back.
+constexpr int H_ROW_BYTES = KH * 2;     // 64 B: features (2 K-chunks) + bias (2 K-chunks)
+constexpr int L_ROW_BYTES = 16 * 2;     // 32 B: features only
+constexpr int A_H_BYTES = QT * H_ROW_BYTES;       // 8 KB
+constexpr int A_L_BYTES = QT * L_ROW_BYTES;       // 4 KB
+constexpr int A_TILE_BYTES = A_H_BYTES + A_L_BYTES;
+constexpr int A_BYTES = NQT * A_TILE_BYTES;       // 48 KB per unit
+constexpr int B_H_BYTES = NT * H_ROW_BYTES;       // 4 KB
+constexpr int B_L_BYTES = NT * L_ROW_BYTES;       // 2 KB
+constexpr int B_X_OFFSET = B_H_BYTES + B_L_BYTES; // original FP32 rows, 64 B each
+constexpr int B_STAGE_BYTES = B_X_OFFSET + NT * FSK_D * 4;   // 10 KB
+constexpr int EPI_WARPS = 4 * NQT;      // one warp per (TMEM lane quarter, query tile)
+constexpr int PRODUCER_WARP = EPI_WARPS;
+constexpr int MMA_WARP = EPI_WARPS + 1;
+constexpr int THREADS = (EPI_WARPS + 2) * 32;
+constexpr int TMEM_COLS = 2 * NQT * NT; // double-buffered accumulators
+constexpr int SMEM_BYTES = A_BYTES + NS * B_STAGE_BYTES + 512;
+// A term is recomputed exactly when it exceeds this fraction of the running
+// sum of its query (including the current chunk's approximate sum).
+constexpr float NEAR_FRACTION = 1.0f / 64.0f;
+constexpr float FP16_TARGET = 8192.0f;  // largest operand magnitude aimed for
+
+static_assert(TMEM_COLS == 512, "TMEM budget");
+static_assert(B_STAGE_BYTES % 16 == 0 && A_BYTES % 16 == 0, "bulk copy granularity");
+
+// Device-side scale state written by the prep kernels (see fsk_tc_kde16.cu).
+struct TcScales {
+  unsigned int qmax_bits, xmax_bits, amax_bits, bmax_bits;  // maxima (FP32 bits, >= 0)
+  float q_scale;   // q' = q_scale * (q - mu)       (= 2 c2 2^eq)
+  float x_scale;   // x' = x_scale * (x - mu)       (= 2^ex)
+  float a_scale;   // alpha part scale  2^-ea  (A bias col holds alpha*a_scale, B holds 1/a_scale)
+  float b_scale;   // beta part scale   2^-eb
+  float out_mul;   // a2 = out_mul * D  (1 unless the product had to be scaled down)
+  int pad[3];
+};
+
+struct TcParams {
+  const uint8_t* qimg;
+  const uint8_t* ximg;
+  const float* qexact;
+  const TcScales* scales;
+  int64_t m, n;
+  int64_t n_tiles;
+  int64_t q_blocks;
+  int64_t splits;
+  int64_t tiles_per_split;
+  float c2, c2_lo, c1;
+  double* partials;
+  double* atomic_acc;
+};
+
+struct TcPlan {
+  int64_t m_pad, n_pad, n_tiles, q_blocks, splits, tiles_per_split;
+  int grid;
+};
+
+TcPlan plan_kde16(int64_t m, int64_t n);
+size_t tc_kde16_ws_bytes(const TcPlan& pl, int64_t m, bool atomic);
+int launch_kde16_tc(const float* q, int64_t m, const float* x, int64_t n, const float* mu, double h,
+                    bool laplace, const TcPlan& pl, WsCarver& c, double** partials_out, bool atomic,
+                    cudaStream_t s);
+int launch_mma_probe(const float* a, const float* b, float* d, cudaStream_t s);
+int launch_wait_timeout_probe(int* out, cudaStream_t s);
+
+// fp16 core-matrix offset of element (row r, k) in an image whose rows are
+// `row_bytes` wide (K = row_bytes / 2).
+__host__ __device__ __forceinline__ uint32_t cm_offset(int r, int k, int row_bytes) {
+  return (uint32_t)(r >> 3) * (uint32_t)(8 * row_bytes) + (uint32_t)(k >> 3) * 128u +
+         (uint32_t)(r & 7) * 16u + (uint32_t)(k & 7) * 2u;
+}
+
+}  // namespace tc
+}  // namespace fsk

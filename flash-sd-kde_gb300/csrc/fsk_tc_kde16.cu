@@ -1,0 +1,619 @@
+// fsk_tc_kde16.cu - tensor-core (tcgen05 / TMEM) 16-D Gaussian KDE, the
+// "fast_tf32" precision mode of the reference, GB300-native.
+//
+// What it computes (per query q_i): sum_j exp(-||q_i - x_j||^2 / (2 h^2)),
+// optionally times the Laplace factor (1 + d/2 - ||q_i-x_j||^2/(2h^2)); the
+// quantity of kernels/kde_eval_16d_stream_splitk.py:14-81 (pass A) and
+// kernels/flash_sd_kde/kde.py:103-144, as FP64 partial sums per data split.
+//
+// How:
+//  * Coordinates are centred on the data mean mu (FP32).  With c2 =
+//    log2(e)/(2h^2), the log2-domain exponent of a pair is
+//        a2 = 2 c2 (q-mu).(x-mu) + beta_j + alpha_i,
+//    beta_j = -c2 |x_j-mu|^2, alpha_i = -c2 |q_i-mu|^2.
+//  * Operands are fp16 pairs v = hi + lo (22 significant bits): queries as
+//    q' = 2 c2 (q-mu) 2^eq, data as x' = (x-mu) 2^ex with power-of-two
+//    scales chosen on the device so every operand stays in fp16 range and
+//    eq + ex = 0 (or the product is scaled down and multiplied back).  Each
+//    hi operand row carries 16 extra "bias" K-columns holding beta_j and
+//    alpha_i as three fp16 parts each against exact powers of two, so one
+//    accumulator D = hi.hi + hi.lo + lo.hi + bias.bias (four tcgen05.mma
+//    kind::f16, M=128, N=64, FP32 accumulation in tensor memory) *is* a2.
+//  * Epilogue: tcgen05.ld one query row per thread, 2^D on the SFU
+//    (ex2.approx), 32-column chunk sums, compensated (TwoSum) per query.
+//  * Exact near-pair recompute: every term above 2^-8 of its query's running
+//    sum (including the current chunk) is recomputed from direct FP32
+//    differences of the original coordinates with the exponent product in
+//    double-float.  Terms never recomputed are each below 2^-8 of the final
+//    sum and carry the ~2^-21 relative error of the fp16x3 product.
+//
+// Pipeline (one persistent CTA per SM, 18 warps):
+//   warp 16 : producer - bulk (TMA) copies of query images per unit and of
+//             data-tile images per stage into shared memory (mbarrier tx).
+//   warp 17 : owns TMEM (512 columns) and issues the MMAs (one lane).
+//   warps 0-15: epilogue; warp w reads TMEM lanes 32*(w%4).. of query tile w/4.
+// A work unit is 512 queries (four M=128 tiles) x one data split; TMEM holds
+// two accumulator buffers x four query tiles x 64 columns.
+#include <cuda_fp16.h>
+
+#include "fsk_kernels.cuh"
+#include "fsk_tc.cuh"
+
+namespace fsk {
+namespace tc {
+
+// ---- idesc / descriptors for fp16 operands ---------------------------------------
+__host__ __device__ constexpr uint32_t idesc_f16_f32(int M, int N) {
+  return (1u << 4)                      // D format F32
+         | (0u << 7) | (0u << 10)       // A, B format F16
+         | (uint32_t(N >> 3) << 17) | (uint32_t(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_f16_ss(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc,
+                                           uint32_t idesc, uint32_t accumulate) {
+  mma_bf16_ss(d_tmem, a_desc, b_desc, idesc, accumulate);  // same instruction, kind::f16
+}
+
+// sum_k (q_k - x_k)^2 from the original FP32 coordinates of data row r.
+__device__ __forceinline__ float exact_dist(const uint8_t* stage, int r, const float (&q)[FSK_D]) {
+  const float4* xr = reinterpret_cast<const float4*>(stage + B_X_OFFSET + r * (FSK_D * 4));
+  float xv[FSK_D];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float4 v = xr[k];
+    xv[4 * k] = v.x; xv[4 * k + 1] = v.y; xv[4 * k + 2] = v.z; xv[4 * k + 3] = v.w;
+  }
+  return sqdist16(q, xv);
+}
+
+template <bool LAPLACE>
+__global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* sA = smem_raw;                               // NQT query tiles: H | L
+  uint8_t* sB = smem_raw + A_BYTES;                     // NS data stages
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + A_BYTES + NS * B_STAGE_BYTES);
+  uint64_t* full = bars;                 // [NS] data stage loaded
+  uint64_t* empty = bars + NS;           // [NS] data stage consumed (MMA + epilogue)
+  uint64_t* tfull = bars + 2 * NS;       // [2] accumulator buffer written
+  uint64_t* tempty = bars + 2 * NS + 2;  // [2] accumulator buffer drained
+  uint64_t* qready = bars + 2 * NS + 4;  // query images loaded
+  uint64_t* qempty = bars + 2 * NS + 5;  // query images no longer read by the MMA
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * NS + 6);
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NS; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1 + EPI_WARPS);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], EPI_WARPS);
+    }
+    mbar_init(qready, 1);
+    mbar_init(qempty, 1);
+    fence_barrier_init();
+  }
+  if (warp == MMA_WARP) {
+    tmem_alloc(tmem_slot, TMEM_COLS);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+  const int64_t units = p.q_blocks * p.splits;
+
+  if (warp == PRODUCER_WARP) {
+    if (lane == 0) {
+      int64_t g = 0, k = 0;
+      for (int64_t u = blockIdx.x; u < units; u += gridDim.x, ++k) {
+        const int64_t qb = u % p.q_blocks, sp = u / p.q_blocks;
+        if (!mbar_wait(qempty, (uint32_t)((k & 1) ^ 1), 1)) goto done;
+        mbar_arrive_expect_tx(qready, A_BYTES);
+        bulk_g2s(sA, p.qimg + qb * (int64_t)A_BYTES, A_BYTES, qready);
+        const int64_t t0 = sp * p.tiles_per_split;
+        const int64_t t1 = imin<int64_t>(p.n_tiles, t0 + p.tiles_per_split);
+        for (int64_t t = t0; t < t1; ++t, ++g) {
+          const int s = (int)(g % NS);
+          if (!mbar_wait(&empty[s], (uint32_t)(((g / NS) & 1) ^ 1), 2)) goto done;
+          mbar_arrive_expect_tx(&full[s], B_STAGE_BYTES);
+          bulk_g2s(sB + s * B_STAGE_BYTES, p.ximg + t * (int64_t)B_STAGE_BYTES, B_STAGE_BYTES, &full[s]);
+        }
+      }
+    }
+  } else if (warp == MMA_WARP) {
+    if (lane == 0) {
+      const uint32_t idesc = idesc_f16_f32(QT, NT);
+      int64_t g = 0, k = 0;
+      for (int64_t u = blockIdx.x; u < units; u += gridDim.x, ++k) {
+        const int64_t sp = u / p.q_blocks;
+        if (!mbar_wait(qready, (uint32_t)(k & 1), 3)) goto done;
+        const int64_t t0 = sp * p.tiles_per_split;
+        const int64_t t1 = imin<int64_t>(p.n_tiles, t0 + p.tiles_per_split);
+        for (int64_t t = t0; t < t1; ++t, ++g) {
+          const int s = (int)(g % NS);
+          const int b = (int)(g & 1);
+          if (!mbar_wait(&full[s], (uint32_t)((g / NS) & 1), 4)) goto done;
+          if (!mbar_wait(&tempty[b], (uint32_t)(((g >> 1) & 1) ^ 1), 5)) goto done;
+          tc_fence_after();
+          const uint32_t bs = smem_u32(sB + s * B_STAGE_BYTES);
+          const uint64_t b_hf = smem_desc_kmajor(bs, 128, 8 * H_ROW_BYTES);
+          const uint64_t b_hb = smem_desc_kmajor(bs + 256, 128, 8 * H_ROW_BYTES);
+          const uint64_t b_l = smem_desc_kmajor(bs + B_H_BYTES, 128, 8 * L_ROW_BYTES);
+#pragma unroll
+          for (int a = 0; a < NQT; ++a) {
+            const uint32_t as = smem_u32(sA + a * A_TILE_BYTES);
+            const uint64_t a_hf = smem_desc_kmajor(as, 128, 8 * H_ROW_BYTES);
+            const uint64_t a_hb = smem_desc_kmajor(as + 256, 128, 8 * H_ROW_BYTES);
+            const uint64_t a_l = smem_desc_kmajor(as + A_H_BYTES, 128, 8 * L_ROW_BYTES);
+            const uint32_t d = tmem_base + (uint32_t)(b * (NQT * NT) + a * NT);
+            mma_f16_ss(d, a_l, b_hf, idesc, 0u);   // lo . hi
+            mma_f16_ss(d, a_hf, b_l, idesc, 1u);   // hi . lo
+            mma_f16_ss(d, a_hf, b_hf, idesc, 1u);  // hi . hi
+            mma_f16_ss(d, a_hb, b_hb, idesc, 1u);  // beta_j + alpha_i
+          }
+          mma_commit(&tfull[b]);
+          mma_commit(&empty[s]);
+        }
+        mma_commit(qempty);
+      }
+    }
+  } else {
+    // ---------------- epilogue warps ----------------
+    const int qt = warp >> 2;          // query tile within the unit
+    const int quarter = warp & 3;      // TMEM lane quarter
+    const int row = quarter * 32 + lane;
+    const uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
+    const float out_mul = p.scales->out_mul;
+    const bool scaled = out_mul != 1.0f;
+    int64_t g = 0;
+    for (int64_t u = blockIdx.x; u < units; u += gridDim.x) {
+      const int64_t qb = u % p.q_blocks, sp = u / p.q_blocks;
+      const int64_t gi = qb * (NQT * QT) + qt * QT + row;   // padded query index
+      float qx[FSK_D];
+#pragma unroll
+      for (int kk = 0; kk < FSK_D; kk += 4) {
+        const float4 v = *reinterpret_cast<const float4*>(p.qexact + gi * FSK_D + kk);
+        qx[kk] = v.x; qx[kk + 1] = v.y; qx[kk + 2] = v.z; qx[kk + 3] = v.w;
+      }
+      Comp acc{0.f, 0.f};
+      float corr = 0.f;
+      const int64_t t0 = sp * p.tiles_per_split;
+      const int64_t t1 = imin<int64_t>(p.n_tiles, t0 + p.tiles_per_split);
+      for (int64_t t = t0; t < t1; ++t, ++g) {
+        const int s = (int)(g % NS);
+        const int b = (int)(g & 1);
+        const int valid = (int)imin<int64_t>(NT, p.n - t * NT);
+        if (!mbar_wait(&tfull[b], (uint32_t)((g >> 1) & 1), 6)) goto done;
+        tc_fence_after();
+        const uint8_t* stage = sB + s * B_STAGE_BYTES;
+#pragma unroll 1
+        for (int c = 0; c < NT / 32; ++c) {
+          uint32_t r[32];
+          tmem_ld32(tmem_base + lane_off + (uint32_t)(b * (NQT * NT) + qt * NT + c * 32), r);
+          tmem_ld_wait();
+          if (c == NT / 32 - 1) {
+            // accumulator buffer fully read into registers: release it
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tempty[b]);
+          }
+          float e[32];
+          if (scaled) {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) e[j] = __uint_as_float(r[j]) * out_mul;
+          } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) e[j] = __uint_as_float(r[j]);
+          }
+          float ps0 = 0.f, ps1 = 0.f, ps2 = 0.f, ps3 = 0.f;
+#pragma unroll
+          for (int j = 0; j < 32; j += 4) {
+            float v0 = ex2_approx(e[j]), v1 = ex2_approx(e[j + 1]);
+            float v2 = ex2_approx(e[j + 2]), v3 = ex2_approx(e[j + 3]);
+            if (LAPLACE) {
+              // 1 + d/2 - dist/(2h^2) = 9 + a2 ln 2   (a2 = -c2 dist)
+              v0 *= fmaf(e[j], 0.69314718055994531f, 1.0f + 0.5f * FSK_D);
+              v1 *= fmaf(e[j + 1], 0.69314718055994531f, 1.0f + 0.5f * FSK_D);
+              v2 *= fmaf(e[j + 2], 0.69314718055994531f, 1.0f + 0.5f * FSK_D);
+              v3 *= fmaf(e[j + 3], 0.69314718055994531f, 1.0f + 0.5f * FSK_D);
+            }
+            e[j] = v0; e[j + 1] = v1; e[j + 2] = v2; e[j + 3] = v3;
+          }
+          if (valid < NT) {  // ragged last data tile: drop padding columns
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+              if (c * 32 + j >= valid) e[j] = 0.f;
+          }
+#pragma unroll
+          for (int j = 0; j < 32; j += 4) {
+            ps0 += e[j]; ps1 += e[j + 1]; ps2 += e[j + 2]; ps3 += e[j + 3];
+          }
+          const float cs = (ps0 + ps1) + (ps2 + ps3);
+          const float thr = (fabsf(acc.s) + fabsf(cs)) * NEAR_FRACTION;
+          bool scan = false;
+#pragma unroll
+          for (int j = 0; j < 32; j += 8) {
+            const float m01 = fmaxf(fabsf(e[j]), fabsf(e[j + 1])), m23 = fmaxf(fabsf(e[j + 2]), fabsf(e[j + 3]));
+            const float m45 = fmaxf(fabsf(e[j + 4]), fabsf(e[j + 5])), m67 = fmaxf(fabsf(e[j + 6]), fabsf(e[j + 7]));
+            scan |= fmaxf(fmaxf(m01, m23), fmaxf(m45, m67)) > thr;
+          }
+          if (scan) {
+            // rare path: every term above the threshold is recomputed exactly
+            uint32_t mask = 0u;
+            float approx_near = 0.f;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              const bool nr = fabsf(e[j]) > thr;
+              mask |= (nr ? 1u : 0u) << j;
+              approx_near += nr ? e[j] : 0.f;
+            }
+            corr -= approx_near;
+            while (mask) {
+              const int j = __ffs(mask) - 1;
+              mask &= mask - 1u;
+              const float dist = exact_dist(stage, c * 32 + j, qx);
+              float ex = exp2_neg_scaled(dist, p.c2, p.c2_lo);
+              if (LAPLACE) ex *= fmaf(-p.c1, dist, 1.0f + 0.5f * FSK_D);
+              corr += ex;
+            }
+          }
+          __syncwarp();
+          acc.add(cs);
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[s]);
+      }
+      if (gi < p.m) {
+        const double v = (double)acc.s + (double)acc.c + (double)corr;
+        if (p.atomic_acc) atomicAdd(&p.atomic_acc[gi], v);
+        else p.partials[sp * p.m + gi] = v;
+      }
+    }
+  }
+done:
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == MMA_WARP) tmem_dealloc(tmem_base, TMEM_COLS);
+}
+
+// ---- prep ----------------------------------------------------------------------------
+__device__ __forceinline__ void atomic_max_pos(unsigned int* addr, float v) {
+  atomicMax(addr, __float_as_uint(fmaxf(v, 0.f)));  // non-negative floats order as integers
+}
+
+// Maxima for the scale selection: |2 c2 (q-mu)|, c2 |q-mu|^2 over queries and
+// |x-mu|, c2 |x-mu|^2 over data.  One thread per row; block-reduced.
+__global__ void scale_stats_kernel(const float* __restrict__ pts, int64_t count, const float* __restrict__ mu,
+                                   float c2, int is_query, TcScales* __restrict__ sc) {
+  float vmax = 0.f, nmax = 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float nrm = 0.f, mx = 0.f;
+#pragma unroll
+    for (int k = 0; k < FSK_D; ++k) {
+      const float v = pts[i * FSK_D + k] - mu[k];
+      nrm = fmaf(v, v, nrm);
+      mx = fmaxf(mx, fabsf(v));
+    }
+    vmax = fmaxf(vmax, is_query ? 2.0f * c2 * mx : mx);
+    nmax = fmaxf(nmax, c2 * nrm);
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, off));
+    nmax = fmaxf(nmax, __shfl_xor_sync(0xffffffffu, nmax, off));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomic_max_pos(is_query ? &sc->qmax_bits : &sc->xmax_bits, vmax);
+    atomic_max_pos(is_query ? &sc->amax_bits : &sc->bmax_bits, nmax);
+  }
+}
+
+__global__ void scale_init_kernel(TcScales* sc) {
+  if (threadIdx.x == 0) {
+    sc->qmax_bits = sc->xmax_bits = sc->amax_bits = sc->bmax_bits = 0u;
+  }
+}
+
+// Chooses the power-of-two scales (one thread).  q' max and x' max are
+// balanced around sqrt(Lq Lx 2^-es) <= FP16_TARGET; alpha and beta parts are
+// scaled into range against exact powers of two (<= 2^15) in the other
+// operand's bias columns.
+__global__ void scale_select_kernel(TcScales* sc) {
+  if (threadIdx.x != 0) return;
+  const float T = FP16_TARGET;
+  float lq = fmaxf(__uint_as_float(sc->qmax_bits), 1e-30f);
+  float lx = fmaxf(__uint_as_float(sc->xmax_bits), 1e-30f);
+  const float am = __uint_as_float(sc->amax_bits), bm = __uint_as_float(sc->bmax_bits);
+  int es = 0;
+  for (int it = 0; it < 64; ++it) {
+    const double prod = (double)lq * (double)lx * ldexp(1.0, -es);
+    const int eaa = am * ldexpf(1.f, -es) > T ? (int)ceil(log2((double)am * ldexp(1.0, -es) / T)) : 0;
+    const int ebb = bm * ldexpf(1.f, -es) > T ? (int)ceil(log2((double)bm * ldexp(1.0, -es) / T)) : 0;
+    if (prod <= (double)T * T && eaa <= 15 && ebb <= 15) break;
+    ++es;
+  }
+  // x' = (x-mu) 2^ex, q' = 2c2 (q-mu) 2^eq, eq + ex = -es, balanced
+  const int ex = (int)floor(0.5 * (log2((double)lq) - log2((double)lx) - es));
+  const int eq = -es - ex;
+  const int ea = am * ldexpf(1.f, -es) > T ? (int)ceil(log2((double)am * ldexp(1.0, -es) / T)) : 0;
+  const int eb = bm * ldexpf(1.f, -es) > T ? (int)ceil(log2((double)bm * ldexp(1.0, -es) / T)) : 0;
+  sc->x_scale = ldexpf(1.f, ex);
+  sc->q_scale = ldexpf(1.f, eq);          // times 2 c2, applied in the prep kernel
+  sc->a_scale = ldexpf(1.f, -es - ea);    // alpha * a_scale in A, 2^ea in B
+  sc->b_scale = ldexpf(1.f, -es - eb);    // beta * b_scale in B, 2^eb in A
+  sc->pad[0] = ea;
+  sc->pad[1] = eb;
+  sc->out_mul = ldexpf(1.f, es);
+}
+
+// Splits v into three fp16 parts (hi, mid, lo) that sum to v to ~33 bits.
+__device__ __forceinline__ void split3_f16(float v, __half& a, __half& b, __half& c) {
+  a = __float2half_rn(v);
+  const float r1 = v - __half2float(a);
+  b = __float2half_rn(r1);
+  c = __float2half_rn(r1 - __half2float(b));
+}
+
+__device__ __forceinline__ void put_h(uint8_t* img, int r, int k, int row_bytes, __half v) {
+  *reinterpret_cast<__half*>(img + cm_offset(r, k, row_bytes)) = v;
+}
+
+// Writes one operand row: H image (features hi + 16 bias columns) and L
+// image (features lo).  bias_own: three parts of this row's own norm term;
+// pow_other: the exact power of two multiplying the other side's parts.
+__device__ __forceinline__ void write_operand_row(uint8_t* h_img, uint8_t* l_img, int r, const float (&v)[FSK_D],
+                                                  float own_term, float pow_other, bool own_first) {
+#pragma unroll
+  for (int k = 0; k < FSK_D; ++k) {
+    const __half hi = __float2half_rn(v[k]);
+    const __half lo = __float2half_rn(v[k] - __half2float(hi));
+    put_h(h_img, r, k, H_ROW_BYTES, hi);
+    put_h(l_img, r, k, L_ROW_BYTES, lo);
+  }
+  __half p0, p1, p2;
+  split3_f16(own_term, p0, p1, p2);
+  const __half one = __float2half_rn(pow_other);
+  const __half zero = __float2half_rn(0.f);
+  // bias columns 16..21: A = [2^eb x3 | alpha parts x3], B = [beta parts x3 | 2^ea x3]
+  const int own = own_first ? 16 : 19, oth = own_first ? 19 : 16;
+  put_h(h_img, r, own + 0, H_ROW_BYTES, p0);
+  put_h(h_img, r, own + 1, H_ROW_BYTES, p1);
+  put_h(h_img, r, own + 2, H_ROW_BYTES, p2);
+  put_h(h_img, r, oth + 0, H_ROW_BYTES, one);
+  put_h(h_img, r, oth + 1, H_ROW_BYTES, one);
+  put_h(h_img, r, oth + 2, H_ROW_BYTES, one);
+#pragma unroll
+  for (int k = 22; k < KH; ++k) put_h(h_img, r, k, H_ROW_BYTES, zero);
+}
+
+// data tile image: [H (NT x 32 fp16) | L (NT x 16 fp16) | x (NT x 16 FP32)]
+__global__ void prep_data_kernel(const float* __restrict__ x, int64_t n, int64_t n_pad,
+                                 const float* __restrict__ mu, float c2, const TcScales* __restrict__ sc,
+                                 uint8_t* __restrict__ img) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n_pad) return;
+  const bool ok = j < n;
+  float xo[FSK_D], v[FSK_D];
+  float nrm = 0.f;
+#pragma unroll
+  for (int k = 0; k < FSK_D; ++k) {
+    xo[k] = ok ? x[j * FSK_D + k] : 0.f;
+    const float cv = xo[k] - mu[k];
+    nrm = fmaf(cv, cv, nrm);
+    v[k] = ok ? cv * sc->x_scale : 0.f;
+  }
+  uint8_t* tile = img + (j / NT) * (int64_t)B_STAGE_BYTES;
+  const int r = (int)(j % NT);
+  const float beta = ok ? -c2 * nrm * sc->b_scale : 0.f;
+  write_operand_row(tile, tile + B_H_BYTES, r, v, beta, ok ? ldexpf(1.f, sc->pad[0]) : 0.f, true);
+  float4* xr = reinterpret_cast<float4*>(tile + B_X_OFFSET + r * (FSK_D * 4));
+#pragma unroll
+  for (int k = 0; k < 4; ++k) xr[k] = make_float4(xo[4 * k], xo[4 * k + 1], xo[4 * k + 2], xo[4 * k + 3]);
+}
+
+// query tile image: [H (QT x 32 fp16) | L (QT x 16 fp16)], plus the original
+// coordinates for the exact recompute.
+__global__ void prep_query_kernel(const float* __restrict__ q, int64_t m, int64_t m_pad,
+                                  const float* __restrict__ mu, float c2, const TcScales* __restrict__ sc,
+                                  uint8_t* __restrict__ img, float* __restrict__ qexact) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m_pad) return;
+  const bool ok = i < m;
+  float qo[FSK_D], v[FSK_D];
+  float nrm = 0.f;
+  const float qs = 2.0f * c2 * sc->q_scale;
+#pragma unroll
+  for (int k = 0; k < FSK_D; ++k) {
+    qo[k] = ok ? q[i * FSK_D + k] : 0.f;
+    const float cv = qo[k] - mu[k];
+    nrm = fmaf(cv, cv, nrm);
+    v[k] = ok ? cv * qs : 0.f;
+  }
+  uint8_t* tile = img + (i / QT) * (int64_t)A_TILE_BYTES;
+  const float alpha = ok ? -c2 * nrm * sc->a_scale : 0.f;
+  write_operand_row(tile, tile + A_H_BYTES, (int)(i % QT), v, alpha, ok ? ldexpf(1.f, sc->pad[1]) : 0.f, false);
+#pragma unroll
+  for (int k = 0; k < FSK_D; ++k) qexact[i * FSK_D + k] = qo[k];
+}
+
+TcPlan plan_kde16(int64_t m, int64_t n) {
+  TcPlan pl;
+  pl.m_pad = (m + NQT * QT - 1) / (NQT * QT) * (NQT * QT);
+  pl.n_tiles = (n + NT - 1) / NT;
+  pl.n_pad = pl.n_tiles * NT;
+  pl.q_blocks = pl.m_pad / (NQT * QT);
+  const int sms = sm_count();
+  // splits: keep a split's data image around 16 MB (L2-resident while every
+  // query block streams it) and give every SM several units.
+  const int64_t l2_tiles = (16ll << 20) / B_STAGE_BYTES;
+  int64_t splits = (pl.n_tiles + l2_tiles - 1) / l2_tiles;
+  const int64_t want_units = 4ll * sms;
+  if (pl.q_blocks * splits < want_units) splits = (want_units + pl.q_blocks - 1) / pl.q_blocks;
+  splits = imax<int64_t>(1, imin<int64_t>(splits, pl.n_tiles));
+  pl.tiles_per_split = (pl.n_tiles + splits - 1) / splits;
+  pl.splits = (pl.n_tiles + pl.tiles_per_split - 1) / pl.tiles_per_split;  // all splits non-empty
+  pl.grid = (int)imin<int64_t>(pl.q_blocks * pl.splits, sms);
+  return pl;
+}
+
+size_t tc_kde16_ws_bytes(const TcPlan& pl, int64_t m, bool atomic) {
+  size_t b = 0;
+  b += align_up(sizeof(TcScales), 256);
+  b += align_up((size_t)pl.q_blocks * A_BYTES, 256);
+  b += align_up((size_t)pl.m_pad * FSK_D * sizeof(float), 256);
+  b += align_up((size_t)pl.n_tiles * B_STAGE_BYTES, 256);
+  b += align_up((size_t)(atomic ? 1 : pl.splits) * m * sizeof(double), 256);
+  return b;
+}
+
+int launch_kde16_tc(const float* q, int64_t m, const float* x, int64_t n, const float* mu, double h,
+                    bool laplace, const TcPlan& pl, WsCarver& c, double** partials_out, bool atomic,
+                    cudaStream_t s) {
+  TcScales* sc = c.take<TcScales>(1);
+  uint8_t* qimg = c.take<uint8_t>((size_t)pl.q_blocks * A_BYTES);
+  float* qexact = c.take<float>((size_t)pl.m_pad * FSK_D);
+  uint8_t* ximg = c.take<uint8_t>((size_t)pl.n_tiles * B_STAGE_BYTES);
+  double* part = c.take<double>((size_t)(atomic ? 1 : pl.splits) * m);
+  if (!c.fits()) return FSK_ERR_WORKSPACE_TOO_SMALL;
+  *partials_out = part;
+
+  const double c2d = FSK_LOG2E / (2.0 * h * h);
+  const float c2 = (float)c2d;
+  const float c2_lo = (float)(c2d - (double)c2);
+  scale_init_kernel<<<1, 32, 0, s>>>(sc);
+  count_launch();
+  const int sblocks_q = (int)imin<int64_t>(1024, (m + 255) / 256);
+  const int sblocks_x = (int)imin<int64_t>(1024, (n + 255) / 256);
+  scale_stats_kernel<<<sblocks_q, 256, 0, s>>>(q, m, mu, c2, 1, sc);
+  count_launch();
+  scale_stats_kernel<<<sblocks_x, 256, 0, s>>>(x, n, mu, c2, 0, sc);
+  count_launch();
+  scale_select_kernel<<<1, 32, 0, s>>>(sc);
+  count_launch();
+  prep_data_kernel<<<(unsigned)((pl.n_pad + 255) / 256), 256, 0, s>>>(x, n, pl.n_pad, mu, c2, sc, ximg);
+  count_launch();
+  prep_query_kernel<<<(unsigned)((pl.m_pad + 255) / 256), 256, 0, s>>>(q, m, pl.m_pad, mu, c2, sc, qimg, qexact);
+  count_launch();
+  if (atomic) launch_zero(part, m, s);
+
+  TcParams p;
+  p.qimg = qimg;
+  p.ximg = ximg;
+  p.qexact = qexact;
+  p.scales = sc;
+  p.m = m;
+  p.n = n;
+  p.n_tiles = pl.n_tiles;
+  p.q_blocks = pl.q_blocks;
+  p.splits = pl.splits;
+  p.tiles_per_split = pl.tiles_per_split;
+  p.c2 = c2;
+  p.c2_lo = c2_lo;
+  p.c1 = (float)(1.0 / (2.0 * h * h));
+  p.partials = atomic ? nullptr : part;
+  p.atomic_acc = atomic ? part : nullptr;
+  cudaError_t e;
+  TimerScope ts(K_KDE16_TC, (double)m * (double)n, s);
+  if (laplace) {
+    e = cudaFuncSetAttribute(kde16_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (e != cudaSuccess) return cuda_status(e);
+    kde16_tc_kernel<true><<<pl.grid, THREADS, SMEM_BYTES, s>>>(p);
+  } else {
+    e = cudaFuncSetAttribute(kde16_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (e != cudaSuccess) return cuda_status(e);
+    kde16_tc_kernel<false><<<pl.grid, THREADS, SMEM_BYTES, s>>>(p);
+  }
+  count_launch();
+  return cuda_status(cudaGetLastError());
+}
+
+// ---- layout probe: D (128 x 64) = A (128 x 32) . B (64 x 32)^T, fp16 ----------------
+// Two K=16 tcgen05.mma steps over the 64-byte-row core-matrix images used by
+// the KDE kernel (the second step at +256 B, like its bias columns).  Inputs
+// are FP32, rounded to fp16 here; D is written row-major FP32.
+__global__ void __launch_bounds__(128, 1) mma_probe_kernel(const float* __restrict__ a,
+                                                           const float* __restrict__ b,
+                                                           float* __restrict__ d) {
+  __shared__ __align__(1024) uint8_t sa[QT * H_ROW_BYTES];
+  __shared__ __align__(1024) uint8_t sb[NT * H_ROW_BYTES];
+  __shared__ uint64_t bar;
+  __shared__ uint32_t slot;
+  const int t = threadIdx.x;
+#pragma unroll 4
+  for (int k = 0; k < KH; ++k) {
+    put_h(sa, t, k, H_ROW_BYTES, __float2half_rn(a[t * KH + k]));
+    if (t < NT) put_h(sb, t, k, H_ROW_BYTES, __float2half_rn(b[t * KH + k]));
+  }
+  if (t == 0) {
+    mbar_init(&bar, 1);
+    fence_barrier_init();
+  }
+  const int warp = t >> 5;
+  if (warp == 0) {
+    tmem_alloc(&slot, 64);
+    tmem_relinquish();
+  }
+  fence_proxy_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = slot;
+  if (t == 0) {
+    const uint32_t idesc = idesc_f16_f32(QT, NT);
+    mma_f16_ss(tbase, smem_desc_kmajor(smem_u32(sa), 128, 8 * H_ROW_BYTES),
+               smem_desc_kmajor(smem_u32(sb), 128, 8 * H_ROW_BYTES), idesc, 0u);
+    mma_f16_ss(tbase, smem_desc_kmajor(smem_u32(sa) + 256, 128, 8 * H_ROW_BYTES),
+               smem_desc_kmajor(smem_u32(sb) + 256, 128, 8 * H_ROW_BYTES), idesc, 1u);
+    mma_commit(&bar);
+  }
+  __syncwarp();
+  const bool ok = mbar_wait(&bar, 0, 20);
+  tc_fence_after();
+  if (ok) {
+    for (int c = 0; c < NT / 32; ++c) {
+      uint32_t r[32];
+      tmem_ld32(tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), r);
+      tmem_ld_wait();
+#pragma unroll
+      for (int j = 0; j < 32; ++j) d[(int64_t)t * NT + c * 32 + j] = __uint_as_float(r[j]);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tbase, 64);
+}
+
+int launch_mma_probe(const float* a, const float* b, float* d, cudaStream_t s) {
+  mma_probe_kernel<<<1, 128, 0, s>>>(a, b, d);
+  count_launch();
+  return cuda_status(cudaGetLastError());
+}
+
+// Waits on an mbarrier that nothing arrives on: the bounded wait gives up
+// (about 2 s), records FSK_ERR_DEVICE_TIMEOUT in the device error word and
+// the kernel returns normally.  Tests the failure path without a GPU fault.
+__global__ void wait_timeout_probe_kernel(int* out) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *out = mbar_wait(&bar, 0, 30) ? 1 : 0;
+}
+
+int launch_wait_timeout_probe(int* out, cudaStream_t s) {
+  wait_timeout_probe_kernel<<<1, 32, 0, s>>>(out);
+  count_launch();
+  return cuda_status(cudaGetLastError());
+}
+
+}  // namespace tc
+}  // namespace fsk

@@ -1,0 +1,119 @@
+"""sklearn-style estimator: drop-in for flash_sd_kde/estimator.py:22-157.
+
+fit(X) resolves the bandwidth (Silverman's rule evaluated on the GPU in FP64),
+stores the data or the SD-KDE-debiased data on the device; score_samples(X)
+returns log(density + eps) as a numpy array, with the log taken in FP64 in
+the kernels' split reduction.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import Literal
+
+import numpy as np
+import torch
+
+from flash_sd_kde.kde import _kde_eval_impl, emp_sd_kde_fit_transform
+from fsk import ops
+from globals import DEFAULT_EPS, DEFAULT_KDE_BACKEND, DEFAULT_PRECISION_MODE, ND_FEATURES
+
+FlashMode = Literal["sd_kde", "kde"]
+BandwidthSpec = float | Literal["silverman"]
+
+
+@dataclass
+class FlashSDKDE:
+    """sklearn-style KDE estimator for Flash-SD-KDE and standard KDE.
+
+    - ``fit(X)`` stores train data (or SD-debiased train data for ``mode="sd_kde"``).
+    - ``score_samples(X)`` returns log density values for each query sample.
+    - ``score(X)`` returns the average log density.
+    ``mode="sd_kde"`` requires 16-D inputs; ``mode="kde"`` accepts 1-D or 16-D.
+    """
+
+    bandwidth: BandwidthSpec = "silverman"
+    mode: FlashMode = "sd_kde"
+    device: str | torch.device = "cuda"
+    precision_mode: str = DEFAULT_PRECISION_MODE
+    kde_backend: str = DEFAULT_KDE_BACKEND
+    emp_score_backend: str | None = None
+    use_precomputed_norms: bool = True
+    autotune: bool = True
+    eps: float = DEFAULT_EPS
+
+    bandwidth_: float | None = field(default=None, init=False)
+    n_features_in_: int | None = field(default=None, init=False)
+    X_fit_: np.ndarray | None = field(default=None, init=False, repr=False)
+    _fit_eval_data: torch.Tensor | None = field(default=None, init=False, repr=False)
+    _is_fitted: bool = field(default=False, init=False, repr=False)
+
+    def fit(self, X: np.ndarray, y=None) -> "FlashSDKDE":
+        del y
+        x_fit = self._validate_input(X)
+        self._validate_mode()
+        self.n_features_in_ = x_fit.shape[1]
+        dev = ops._device(self.device)
+        x_dev = torch.from_numpy(x_fit).to(dev)
+        self.bandwidth_ = self._resolve_bandwidth(x_dev)
+        self.X_fit_ = x_fit
+        if self.mode == "sd_kde":
+            if self.n_features_in_ != ND_FEATURES:
+                raise ValueError(
+                    f'mode="sd_kde" currently requires {ND_FEATURES} features, but got {self.n_features_in_}.'
+                )
+            self._fit_eval_data = emp_sd_kde_fit_transform(
+                x_dev, self.bandwidth_, device=dev, precision_mode=self.precision_mode,
+                emp_score_backend=self.emp_score_backend, use_precomputed_norms=self.use_precomputed_norms,
+                autotune=self.autotune, eps=self.eps)
+        else:
+            self._fit_eval_data = x_dev[:, 0].contiguous() if self.n_features_in_ == 1 else x_dev
+        self._is_fitted = True
+        return self
+
+    def score_samples(self, X: np.ndarray) -> np.ndarray:
+        self._check_is_fitted()
+        queries = self._validate_input(X)
+        if queries.shape[1] != self.n_features_in_:
+            raise ValueError(
+                f"X has {queries.shape[1]} features, but estimator was fitted with {self.n_features_in_} features."
+            )
+        dev = ops._device(self.device)
+        q = torch.from_numpy(queries).to(dev)
+        if self.n_features_in_ == 1:
+            q = q[:, 0].contiguous()
+        log_density = _kde_eval_impl(self._fit_eval_data, q, self.bandwidth_, device=dev,
+                                     precision_mode=self.precision_mode, kde_backend=self.kde_backend,
+                                     apply_laplacian_correction=False, log_eps=float(self.eps))
+        return log_density.detach().cpu().numpy()
+
+    def score(self, X: np.ndarray, y=None) -> float:
+        del y
+        return float(np.mean(self.score_samples(X)))
+
+    def _validate_input(self, X: np.ndarray) -> np.ndarray:
+        arr = np.ascontiguousarray(np.asarray(X, dtype=np.float32))
+        if arr.ndim != 2:
+            raise ValueError("Expected X with shape (n_samples, n_features), consistent with sklearn.")
+        if arr.shape[0] == 0:
+            raise ValueError("X must contain at least one sample.")
+        if arr.shape[1] == 0:
+            raise ValueError("X must contain at least one feature.")
+        return arr
+
+    def _resolve_bandwidth(self, x_dev: torch.Tensor) -> float:
+        if isinstance(self.bandwidth, str):
+            if self.bandwidth != "silverman":
+                raise ValueError(f"Unsupported bandwidth='{self.bandwidth}'. Use float or 'silverman'.")
+            return float(ops.silverman(x_dev).item())
+        bw = float(self.bandwidth)
+        if bw <= 0:
+            raise ValueError("bandwidth must be positive.")
+        return bw
+
+    def _validate_mode(self) -> None:
+        if self.mode not in {"sd_kde", "kde"}:
+            raise ValueError(f"Unsupported mode='{self.mode}'. Expected one of ['sd_kde', 'kde'].")
+
+    def _check_is_fitted(self) -> None:
+        if not self._is_fitted:
+            raise ValueError("Estimator is not fitted. Call fit(X) before score_samples(X).")

@@ -1,0 +1,86 @@
+"""Builds libfsk.so in-tree from csrc/*.cu for sm_103a (GB300).
+
+Each translation unit is compiled by its own nvcc process (in parallel), then
+linked with ``nvcc -shared``.  The CUDA runtime is linked statically so the
+library does not depend on the exact libcudart the host process has loaded.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+PKG_ROOT = Path(__file__).resolve().parent.parent          # flash-sd-kde_gb300/
+CSRC = PKG_ROOT / "csrc"
+INCLUDE = PKG_ROOT.parent / "include"
+BUILD_DIR = PKG_ROOT / "_build"
+LIB_PATH = Path(__file__).resolve().parent / "libfsk.so"
+
+ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = [
+    "-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr",
+    "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+    "-rdc=true",
+]
+
+
+def _nvcc() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found; the CUDA 13 toolkit is required to build libfsk.so")
+
+
+def sources() -> list[Path]:
+    return sorted(CSRC.glob("*.cu"))
+
+
+def _stale(extra_flags: list[str]) -> bool:
+    if not LIB_PATH.exists():
+        return True
+    stamp = BUILD_DIR / "flags.txt"
+    if not stamp.exists() or stamp.read_text() != " ".join(NVCC_FLAGS + extra_flags):
+        return True
+    lib_mtime = LIB_PATH.stat().st_mtime
+    deps = list(CSRC.glob("*")) + list(INCLUDE.glob("*.h"))
+    return any(p.stat().st_mtime > lib_mtime for p in deps)
+
+
+def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | None = None) -> Path:
+    """Compile every csrc/*.cu for sm_103a and link libfsk.so; returns its path."""
+    extra_flags = list(extra_flags or [])
+    if not force and not _stale(extra_flags):
+        return LIB_PATH
+    nvcc = _nvcc()
+    BUILD_DIR.mkdir(exist_ok=True)
+    srcs = sources()
+
+    def compile_one(src: Path) -> Path:
+        obj = BUILD_DIR / (src.stem + ".o")
+        cmd = [nvcc, *ARCH_FLAGS, *NVCC_FLAGS, *extra_flags, f"-I{INCLUDE}", "-c", str(src), "-o", str(obj)]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {src.name}:\n{res.stdout}\n{res.stderr}")
+        if verbose and (res.stdout or res.stderr):
+            sys.stderr.write(res.stdout + res.stderr)
+        return obj
+
+    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+        objs = list(ex.map(compile_one, srcs))
+    tmp = LIB_PATH.with_suffix(".so.tmp")
+    cmd = [nvcc, *ARCH_FLAGS, "-rdc=true", "-shared", "-o", str(tmp), *map(str, objs)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+    os.replace(tmp, LIB_PATH)
+    (BUILD_DIR / "flags.txt").write_text(" ".join(NVCC_FLAGS + extra_flags))
+    return LIB_PATH
+
+
+if __name__ == "__main__":
+    v = "-v" in sys.argv
+    extra = ["-Xptxas", "-v"] if "--ptxas-v" in sys.argv else []
+    print(build(force=True, verbose=v or bool(extra), extra_flags=extra))

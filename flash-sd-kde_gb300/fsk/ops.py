@@ -1,0 +1,255 @@
+"""Tensor-level wrappers over the libfsk C ABI.
+
+Every op takes CUDA float32 tensors (converted with ``.to(device, float32,
+copy=False).contiguous()`` like the reference's ``_to_matrix_tensor``), takes
+its device workspace from torch's caching allocator, enqueues the kernels on
+the current torch stream of the tensors' device and returns new tensors.
+Nothing here runs on the CPU: a missing extension or a non-CUDA device is an
+error.
+"""
+from __future__ import annotations
+
+import math
+from typing import Sequence
+
+import torch
+
+from . import _lib as L
+
+ND_FEATURES = 16
+
+
+def _device(device) -> torch.device:
+    dev = torch.device(device)
+    if dev.type != "cuda":
+        raise ValueError("the GB300 kernels require a CUDA device.")
+    if not torch.cuda.is_available():
+        raise RuntimeError("CUDA is not available but was requested.")
+    if dev.index is None:
+        dev = torch.device("cuda", torch.cuda.current_device())
+    return dev
+
+
+def as_matrix(x: Sequence[Sequence[float]] | torch.Tensor, device: torch.device, dim: int = ND_FEATURES) -> torch.Tensor:
+    if isinstance(x, torch.Tensor):
+        t = x.to(device=device, dtype=torch.float32, copy=False)
+    else:
+        t = torch.as_tensor(x, dtype=torch.float32, device=device)
+    if t.ndim != 2 or t.shape[1] != dim:
+        raise ValueError(f"expected tensor with shape (n, {dim}), got {tuple(t.shape)}")
+    return t.contiguous()
+
+
+def as_vector(x: Sequence[float] | torch.Tensor, device: torch.device) -> torch.Tensor:
+    if isinstance(x, torch.Tensor):
+        t = x.to(device=device, dtype=torch.float32, copy=False)
+    else:
+        t = torch.as_tensor(x, dtype=torch.float32, device=device)
+    if t.ndim != 1:
+        raise ValueError("expected a 1D tensor.")
+    return t.contiguous()
+
+
+def _ptr(t: torch.Tensor | None):
+    return None if t is None else t.data_ptr()
+
+
+def _stream(device: torch.device) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def _workspace(nbytes: int, device: torch.device) -> torch.Tensor:
+    return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+
+
+def _check_bw(h: float) -> float:
+    h = float(h)
+    if not (h > 0.0) or not math.isfinite(h):
+        raise ValueError("bandwidth must be positive.")
+    return h
+
+
+def kde16_sum(
+    queries: torch.Tensor,
+    data: torch.Tensor,
+    bandwidth: float,
+    *,
+    precision: str = "tensor",
+    laplace: bool = False,
+    atomic: bool = False,
+    out_scale: float = 1.0,
+    log_eps: float | None = None,
+    out: torch.Tensor | None = None,
+) -> torch.Tensor:
+    """out[i] = out_scale * sum_j phi(q_i, x_j)  (or log(out_scale*sum + log_eps))."""
+    h = _check_bw(bandwidth)
+    dev = _device(queries.device)
+    q = as_matrix(queries, dev)
+    x = as_matrix(data, dev)
+    m, n = q.shape[0], x.shape[0]
+    if m == 0 or n == 0:
+        raise ValueError("data and queries must contain at least one sample.")
+    flags = (L.FSK_PREC_IEEE if precision == "ieee" else L.FSK_PREC_TENSOR)
+    flags |= (L.FSK_LAPLACE if laplace else 0) | (L.FSK_ATOMIC if atomic else 0)
+    if log_eps is not None:
+        flags |= L.FSK_OUT_LOG
+    lib = L.load()
+    with torch.cuda.device(dev):
+        if out is None:
+            out = torch.empty(m, dtype=torch.float32, device=dev)
+        ws_bytes = lib.fsk_kde16_workspace_bytes(m, n, flags)
+        ws = _workspace(ws_bytes, dev)
+        st = lib.fsk_kde16(q.data_ptr(), m, x.data_ptr(), n, h, flags, float(out_scale),
+                           float(log_eps or 0.0), out.data_ptr(), ws.data_ptr(), ws.numel(), _stream(dev))
+    L.check(st, "fsk_kde16")
+    return out
+
+
+def empscore16(
+    data: torch.Tensor,
+    bandwidth: float,
+    *,
+    variant: str = "ordered",
+    feature_major: bool = False,
+) -> tuple[torch.Tensor, torch.Tensor]:
+    """(pdf_sum (n,), weighted_sum (n,16)); feature_major returns a (16,n)-backed view."""
+    h = _check_bw(bandwidth)
+    dev = _device(data.device)
+    x = as_matrix(data, dev)
+    n = x.shape[0]
+    if n == 0:
+        raise ValueError("data must contain at least one element.")
+    var = L.FSK_SCORE_SYMMETRIC if variant == "symmetric" else L.FSK_SCORE_ORDERED
+    flags = L.FSK_WEIGHTED_FEATURE_MAJOR if feature_major else 0
+    lib = L.load()
+    with torch.cuda.device(dev):
+        pdf = torch.empty(n, dtype=torch.float32, device=dev)
+        w = torch.empty((ND_FEATURES, n) if feature_major else (n, ND_FEATURES), dtype=torch.float32, device=dev)
+        ws = _workspace(lib.fsk_empscore16_workspace_bytes(n, var, flags), dev)
+        st = lib.fsk_empscore16(x.data_ptr(), n, h, var, flags, pdf.data_ptr(), w.data_ptr(), ws.data_ptr(),
+                                ws.numel(), _stream(dev))
+    L.check(st, "fsk_empscore16")
+    return pdf, (w.t() if feature_major else w)
+
+
+def debias16(
+    data: torch.Tensor,
+    pdf_sum: torch.Tensor,
+    weighted_sum: torch.Tensor,
+    bandwidth: float,
+    eps: float,
+    *,
+    return_score: bool = False,
+):
+    """x + h^2/2 * score with score = (W/(pdf+eps) - x)/h^2, computed in FP64."""
+    h = _check_bw(bandwidth)
+    dev = _device(data.device)
+    x = as_matrix(data, dev)
+    n = x.shape[0]
+    pdf = pdf_sum.to(device=dev, dtype=torch.float32).contiguous()
+    w = weighted_sum.to(device=dev, dtype=torch.float32)
+    if w.shape != (n, ND_FEATURES) or pdf.shape != (n,):
+        raise ValueError("pdf_sum must be (n,) and weighted_sum (n, 16).")
+    lib = L.load()
+    with torch.cuda.device(dev):
+        deb = torch.empty_like(x)
+        score = torch.empty_like(x) if return_score else None
+        st = lib.fsk_debias16(x.data_ptr(), n, pdf.data_ptr(), w.data_ptr(), w.stride(0), w.stride(1), h,
+                              float(eps), deb.data_ptr(), _ptr(score), _stream(dev))
+    L.check(st, "fsk_debias16")
+    return (deb, score) if return_score else deb
+
+
+def kde1d_sum(
+    queries: torch.Tensor,
+    data: torch.Tensor,
+    bandwidth: float,
+    *,
+    laplace: bool = False,
+    atomic: bool = False,
+    out_scale: float = 1.0,
+    log_eps: float | None = None,
+) -> torch.Tensor:
+    h = _check_bw(bandwidth)
+    dev = _device(queries.device)
+    q = as_vector(queries, dev)
+    x = as_vector(data, dev)
+    m, n = q.numel(), x.numel()
+    if m == 0 or n == 0:
+        raise ValueError("data and queries must be non-empty.")
+    flags = (L.FSK_LAPLACE if laplace else 0) | (L.FSK_ATOMIC if atomic else 0)
+    if log_eps is not None:
+        flags |= L.FSK_OUT_LOG
+    lib = L.load()
+    with torch.cuda.device(dev):
+        out = torch.empty(m, dtype=torch.float32, device=dev)
+        ws = _workspace(lib.fsk_kde1d_workspace_bytes(m, n, flags), dev)
+        st = lib.fsk_kde1d(q.data_ptr(), m, x.data_ptr(), n, h, flags, float(out_scale), float(log_eps or 0.0),
+                           out.data_ptr(), ws.data_ptr(), ws.numel(), _stream(dev))
+    L.check(st, "fsk_kde1d")
+    return out
+
+
+def kde1d_score(queries: torch.Tensor, data: torch.Tensor, bandwidth: float):
+    """(score, pdf, deriv) of the 1-D Gaussian KDE at the queries."""
+    h = _check_bw(bandwidth)
+    dev = _device(queries.device)
+    q = as_vector(queries, dev)
+    x = as_vector(data, dev)
+    m, n = q.numel(), x.numel()
+    if m == 0 or n == 0:
+        raise ValueError("data and queries must be non-empty.")
+    lib = L.load()
+    with torch.cuda.device(dev):
+        score = torch.empty(m, dtype=torch.float32, device=dev)
+        pdf = torch.empty_like(score)
+        deriv = torch.empty_like(score)
+        ws = _workspace(lib.fsk_kde1d_workspace_bytes(m, n, 0), dev)
+        st = lib.fsk_kde1d_score(q.data_ptr(), m, x.data_ptr(), n, h, score.data_ptr(), pdf.data_ptr(),
+                                 deriv.data_ptr(), ws.data_ptr(), ws.numel(), _stream(dev))
+    L.check(st, "fsk_kde1d_score")
+    return score, pdf, deriv
+
+
+def silverman(data: torch.Tensor, *, rule: str = "silverman") -> torch.Tensor:
+    """Bandwidth as a 0-d FP64 CUDA tensor (rule 'silverman' or 'sdkde_1d')."""
+    dev = _device(data.device)
+    x = data.to(device=dev, dtype=torch.float32, copy=False)
+    if x.ndim == 1:
+        x = x[:, None]
+    if x.ndim != 2:
+        raise ValueError("data must be 1D or 2D.")
+    x = x.contiguous()
+    n, d = x.shape
+    if n == 0:
+        raise ValueError("data must contain at least one element.")
+    r = L.FSK_RULE_SDKDE_1D if rule == "sdkde_1d" else L.FSK_RULE_SILVERMAN
+    lib = L.load()
+    with torch.cuda.device(dev):
+        h = torch.empty((), dtype=torch.float64, device=dev)
+        ws = _workspace(lib.fsk_silverman_workspace_bytes(n, d), dev)
+        st = lib.fsk_silverman(x.data_ptr(), n, d, r, h.data_ptr(), ws.data_ptr(), ws.numel(), _stream(dev))
+    L.check(st, "fsk_silverman")
+    return h
+
+
+def device_status(device=None) -> None:
+    """Synchronise and raise if a bounded in-kernel wait recorded a timeout."""
+    dev = _device(device if device is not None else "cuda")
+    with torch.cuda.device(dev):
+        st = L.load().fsk_device_status(_stream(dev))
+    L.check(st, "device status")
+
+
+def mma_probe(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
+    """tcgen05.mma of fp16(a) (128,32) by fp16(b) (64,32)^T -> (128,64) FP32."""
+    dev = _device(a.device)
+    a = a.to(device=dev, dtype=torch.float32).contiguous()
+    b = b.to(device=dev, dtype=torch.float32).contiguous()
+    if a.shape != (128, 32) or b.shape != (64, 32):
+        raise ValueError("probe operands must be (128, 32) and (64, 32)")
+    with torch.cuda.device(dev):
+        d = torch.empty((128, 64), dtype=torch.float32, device=dev)
+        st = L.load().fsk_diag_mma_probe(a.data_ptr(), b.data_ptr(), d.data_ptr(), _stream(dev))
+    L.check(st, "fsk_diag_mma_probe")
+    return d

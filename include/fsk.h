@@ -1,0 +1,186 @@
+/*
+ * fsk.h - C ABI of the GB300 (sm_103a) Flash-SD-KDE hot path.
+ *
+ * Every entry point takes plain device pointers, element counts, a bandwidth,
+ * option flags, a caller-owned device workspace and a CUDA stream (passed as
+ * void*, i.e. a cudaStream_t / CUstream; NULL means the legacy default
+ * stream).  Nothing here allocates device memory except where stated, nothing
+ * synchronises the stream, and nothing falls back to the CPU.  Each call
+ * returns an fsk_status code; FSK_ERR_INVALID_ARGUMENT corresponds to the
+ * reference's ValueError, every other non-zero code to its RuntimeError.
+ *
+ * Layouts: 16-D point sets are row-major (n, 16) float32 with a 64-byte row
+ * stride, contiguous, 16-byte aligned; 1-D sets are contiguous float32.
+ *
+ * Reference interfaces replaced (paths inside the Flash-SD-KDE project):
+ *   fsk_kde16        kernels/kde_eval_16d_stream_splitk.py:263 (kde_eval_16d_splitk),
+ *                    :373 (kde_eval_16d_atomic), kernels/flash_sd_kde/kde.py:374
+ *                    (gaussian_kde_triton_nd) and the normalisation in
+ *                    flash_sd_kde/kde.py:119-122
+ *   fsk_empscore16   kernels/flash_sd_kde/empirical.py:134 (emp_score_16d_flash_sd_kde),
+ *                    kernels/emp_score_16d_ordered_splitk.py:162,
+ *                    kernels/emp_score_16d_symmetric_atomic.py:163, with the
+ *                    partial reduction of kernels/reduce_partials.py:61-108
+ *   fsk_debias16     flash_sd_kde/kde.py:319-322 and
+ *                    kernels/flash_sd_kde/empirical.py:280-283
+ *   fsk_kde1d        kernels/kde_eval_1d_splitk.py:141 (kde_eval_1d_splitk), :222
+ *                    (kde_eval_1d_atomic), kernels/flash_sd_kde/kde.py:147
+ *                    (gaussian_kde_triton) and flash_sd_kde/kde.py:93-94
+ *   fsk_kde1d_score  kernels/flash_sd_kde/kde.py:348 (gaussian_kde_score_triton)
+ *   fsk_silverman    flash_sd_kde/reference.py:171-184 (silverman_bandwidth_nd),
+ *                    :24-36 (silverman_bandwidth), and the 1-D SD-KDE rule of
+ *                    kernels/flash_sd_kde/empirical.py:328-333
+ */
+#ifndef FSK_H_
+#define FSK_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define FSK_API __attribute__((visibility("default")))
+#else
+#define FSK_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum fsk_status {
+  FSK_OK = 0,
+  FSK_ERR_INVALID_ARGUMENT = 1,   /* bad size, pointer, bandwidth or flag   */
+  FSK_ERR_WORKSPACE_TOO_SMALL = 2,
+  FSK_ERR_CUDA = 3,               /* a CUDA runtime call failed             */
+  FSK_ERR_DEVICE_TIMEOUT = 4,     /* a bounded in-kernel wait gave up       */
+  FSK_ERR_UNSUPPORTED_DEVICE = 5, /* not an sm_103 device                   */
+  FSK_ERR_SCRATCH_LIMIT = 6       /* request exceeds a fixed scratch limit  */
+};
+
+/* ---- option flags ------------------------------------------------------ */
+/* precision_mode "fast_tf32" of the reference: tensor-core split-precision
+ * distance products (fp16 hi/lo pairs, three products, FP32 accumulation,
+ * norms folded into the accumulator) and an exact FP32 direct-difference
+ * recompute of every pair that carries more than 1/64 of its query's running
+ * sum.  This is the default (value 0). */
+#define FSK_PREC_TENSOR 0x0
+/* precision_mode "fp32_ieee": every pair by FP32 direct differences on the
+ * CUDA cores, no tensor cores. */
+#define FSK_PREC_IEEE 0x1
+/* Laplace-corrected ("linearized") kernel phi * (1 + d/2 - dist/(2 h^2)),
+ * kernels/kde_eval_16d_stream_splitk.py:75-76. */
+#define FSK_LAPLACE 0x2
+/* Write out = log(out_scale * sum + out_eps) instead of out_scale * sum. */
+#define FSK_OUT_LOG 0x4
+/* Reduce splits with FP64 atomics instead of the ordered partial buffer
+ * (kde_backend="atomic" / emp_score_backend="symmetric_atomic"). */
+#define FSK_ATOMIC 0x8
+/* fsk_empscore16: write weighted_sum as a (16, n) buffer, the layout of the
+ * reference's flash backend (kernels/flash_sd_kde/empirical.py:180,223). */
+#define FSK_WEIGHTED_FEATURE_MAJOR 0x10
+
+/* empirical-score accumulation variants */
+#define FSK_SCORE_ORDERED 0   /* deterministic split-K, fixed-order FP64 reduce */
+#define FSK_SCORE_SYMMETRIC 1 /* triangle tiles, phi_ij = phi_ji, half the exps */
+
+/* Silverman rules */
+#define FSK_RULE_SILVERMAN 0  /* 0.9 * mean_k min(std_k, IQR_k/1.34) * n^(-1/(d+4)) */
+#define FSK_RULE_SDKDE_1D 1   /* 0.4 * min(std, IQR/1.34) * n^(-1/9), 1-D only     */
+
+/* ---- 16-D Gaussian KDE ------------------------------------------------- */
+/* out[i] = out_scale * sum_j phi(q_i, x_j), phi = exp(-||q_i - x_j||^2 / (2 h^2))
+ * (times the Laplace factor with FSK_LAPLACE); the sum is accumulated per
+ * split with compensated FP32 and reduced across splits in FP64, and the
+ * scale (and log) is applied in FP64.  m, n >= 1. */
+FSK_API size_t fsk_kde16_workspace_bytes(int64_t m, int64_t n, int flags);
+FSK_API int fsk_kde16(const float* queries, int64_t m, const float* data, int64_t n,
+              double bandwidth, int flags, double out_scale, double out_eps,
+              float* out, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- 16-D empirical-score accumulators --------------------------------- */
+/* pdf_sum[i] = sum_j phi_ij, weighted_sum[i,:] = sum_j phi_ij x_j, the
+ * self-pair included (flash_sd_kde/reference.py:263-284). */
+FSK_API size_t fsk_empscore16_workspace_bytes(int64_t n, int variant, int flags);
+FSK_API int fsk_empscore16(const float* data, int64_t n, double bandwidth, int variant,
+                   int flags, float* pdf_sum, float* weighted_sum,
+                   void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- one-step SD-KDE debias shift -------------------------------------- */
+/* score = (W / (pdf + eps) - x) / h^2, debiased = x + h^2/2 * score, in FP64.
+ * weighted_sum element (i, k) is read at weighted_sum[i*w_row_stride + k*w_col_stride].
+ * score may be NULL. */
+FSK_API int fsk_debias16(const float* data, int64_t n, const float* pdf_sum,
+                 const float* weighted_sum, int64_t w_row_stride,
+                 int64_t w_col_stride, double bandwidth, double eps,
+                 float* debiased, float* score, void* stream);
+
+/* ---- 1-D Gaussian KDE and KDE score ------------------------------------ */
+FSK_API size_t fsk_kde1d_workspace_bytes(int64_t m, int64_t n, int flags);
+FSK_API int fsk_kde1d(const float* queries, int64_t m, const float* data, int64_t n,
+              double bandwidth, int flags, double out_scale, double out_eps,
+              float* out, void* workspace, size_t workspace_bytes, void* stream);
+/* pdf[i] = sum_j phi(z)/(n h sqrt(2 pi)), deriv[i] = sum_j -z phi(z)/(n h^2 sqrt(2 pi)),
+ * score[i] = deriv[i] / (pdf[i] + 1e-12), z = (q_i - x_j)/h.  Any output may be NULL. */
+FSK_API int fsk_kde1d_score(const float* queries, int64_t m, const float* data, int64_t n,
+                    double bandwidth, float* score, float* pdf, float* deriv,
+                    void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- bandwidth rules ----------------------------------------------------- */
+/* Writes the bandwidth (FP64) to the device scalar h_out.  Per-axis mean,
+ * standard deviation and the 25th/75th percentiles (linear interpolation,
+ * as numpy.percentile) are computed on the GPU in FP64 / exact selection. */
+FSK_API size_t fsk_silverman_workspace_bytes(int64_t n, int d);
+FSK_API int fsk_silverman(const float* data, int64_t n, int d, int rule, double* h_out,
+                  void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- split reduction ------------------------------------------------------ */
+/* out[i] = sum_s partials[s * count + i] over a (splits, count) FP32 buffer,
+ * accumulated in FP64 in split order.  Replaces reduce_pdf_partials and
+ * reduce_weighted_partials (kernels/reduce_partials.py:61-108), which sum in
+ * FP32. */
+FSK_API int fsk_reduce_partials(const float* partials, int64_t splits, int64_t count,
+                                float* out, void* stream);
+
+/* ---- diagnostics --------------------------------------------------------- */
+/* Synchronises the stream, reads and clears the library's device error word.
+ * Returns FSK_OK, FSK_ERR_DEVICE_TIMEOUT or FSK_ERR_CUDA. */
+FSK_API int fsk_device_status(void* stream);
+FSK_API const char* fsk_strerror(int status);
+FSK_API int fsk_version(void);
+/* Number of this library's kernel launches since load (monotonic counter). */
+FSK_API int64_t fsk_launch_count(void);
+
+/* Tensor-core layout probe, no counterpart in the reference: two K=16
+ * tcgen05.mma steps (fp16 inputs, FP32 accumulate, M=128, N=64) of
+ * a (128,32) by b (64,32)^T over the 64-byte-row operand images the KDE
+ * kernel uses; inputs are FP32 rounded to fp16, d is (128,64) FP32
+ * row-major.  The tests compare it with a host dot product. */
+FSK_API int fsk_diag_mma_probe(const float* a, const float* b, float* d, void* stream);
+/* Failure-path probe, no counterpart in the reference: a kernel waits on an
+ * mbarrier nothing arrives on; its bounded wait gives up after about 2 s,
+ * writes 0 to *out (device int) and records FSK_ERR_DEVICE_TIMEOUT, which the
+ * next fsk_device_status returns (and clears). */
+FSK_API int fsk_diag_wait_timeout_probe(int* out, void* stream);
+/* Roofline inputs, no counterpart in the reference: sustained device rates
+ * (operations / s) of ex2.approx.f32 (SFU), fma.rn.f32 and fma.rn.f32x2
+ * (counted as two FMAs), written to the host array rates_out[3].  Allocates
+ * a small device buffer and synchronises the stream (diagnostics only). */
+FSK_API int fsk_diag_pipe_rates(double* rates_out, void* stream);
+
+/* ---- measurement hooks (no counterpart in the reference) ------------------ */
+/* Kernel ids: 1 tensor-core 16-D KDE, 2 CUDA-core 16-D KDE, 3 CUDA-core
+ * ordered score, 4 CUDA-core symmetric score, 5 1-D KDE, 6 1-D KDE score,
+ * 7 tensor-core ordered score, 8 tensor-core symmetric score. */
+/* When enabled, each hot-path kernel launch is bracketed by CUDA events on
+ * its own stream. */
+FSK_API void fsk_timer_enable(int on);
+/* Per kernel id since the last call: launches, device ms and pair
+ * evaluations, into host arrays of `cap` rows; returns the row count (or a
+ * negated status).  Waits for the recorded events. */
+FSK_API int fsk_timer_collect(int* ids, int64_t* launches, double* ms, double* work, int cap);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FSK_H_ */

@@ -1,0 +1,105 @@
+"""FP64 log-space ground truth -- test infrastructure only.
+
+Restates experiments/error_suite_16d/reference.py:32-82 of the reference
+project: log p(y) = logsumexp_j(-||y - x_j||^2 / (2h^2)) + log_const with
+log_const = -log n - d log h - (d/2) log(2 pi), accumulated chunk by chunk
+with a running logaddexp.  The distance is formed from direct FP64
+differences (exact enough that the FP64 expansion's cancellation does not
+matter).  Also FP64 versions of the empirical score and the debias shift.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+def _logaddexp(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    return np.logaddexp(a, b)
+
+
+def log_density(samples, queries, bandwidth: float, *, laplace: bool = False,
+                q_chunk: int = 512, s_chunk: int = 8192) -> np.ndarray:
+    """FP64 log-density of the Gaussian KDE (reference :32-82).  With
+    laplace=True returns log |sum phi (1 + d/2 - dist/(2h^2))| (the corrected
+    sum can be negative; tests compare densities for that case)."""
+    x = np.asarray(samples, dtype=np.float64)
+    q = np.asarray(queries, dtype=np.float64)
+    if x.ndim == 1:
+        x = x[:, None]
+    if q.ndim == 1:
+        q = q[:, None]
+    n, d = x.shape
+    log_const = -math.log(n) - d * math.log(bandwidth) - 0.5 * d * math.log(2.0 * math.pi)
+    out = np.empty(q.shape[0], dtype=np.float64)
+    inv2h2 = 1.0 / (2.0 * bandwidth * bandwidth)
+    for qs in range(0, q.shape[0], q_chunk):
+        qb = q[qs:qs + q_chunk]
+        run = np.full(qb.shape[0], -np.inf)
+        lap = np.zeros(qb.shape[0]) if laplace else None
+        for ss in range(0, n, s_chunk):
+            xb = x[ss:ss + s_chunk]
+            dist = np.zeros((qb.shape[0], xb.shape[0]))
+            for k in range(d):
+                diff = qb[:, k:k + 1] - xb[None, :, k]
+                dist += diff * diff
+            expo = -dist * inv2h2
+            if laplace:
+                lap += (np.exp(expo) * (1.0 + 0.5 * d + expo)).sum(axis=1)
+            else:
+                mx = expo.max(axis=1)
+                lse = mx + np.log(np.exp(expo - mx[:, None]).sum(axis=1))
+                run = _logaddexp(run, lse)
+        out[qs:qs + q_chunk] = (np.log(np.abs(lap)) if laplace else run) + log_const
+    return out
+
+
+def density(samples, queries, bandwidth: float, **kw) -> np.ndarray:
+    return np.exp(log_density(samples, queries, bandwidth, **kw))
+
+
+def empirical_score(data, bandwidth: float, *, eps: float = 1e-12, chunk: int = 2048):
+    """FP64 (pdf_sum, weighted_sum, score) of reference.py:263-284."""
+    x = np.asarray(data, dtype=np.float64)
+    n = x.shape[0]
+    pdf = np.zeros(n)
+    w = np.zeros_like(x)
+    inv2h2 = 1.0 / (2.0 * bandwidth * bandwidth)
+    for s in range(0, n, chunk):
+        xb = x[s:s + chunk]
+        dist = np.zeros((n, xb.shape[0]))
+        for k in range(x.shape[1]):
+            diff = x[:, k:k + 1] - xb[None, :, k]
+            dist += diff * diff
+        phi = np.exp(-dist * inv2h2)
+        pdf += phi.sum(axis=1)
+        w += phi @ xb
+    score = (w / (pdf[:, None] + eps) - x) / (bandwidth * bandwidth)
+    return pdf, w, score
+
+
+def debias(data, bandwidth: float, *, eps: float = 1e-12) -> np.ndarray:
+    _, _, score = empirical_score(data, bandwidth, eps=eps)
+    return np.asarray(data, dtype=np.float64) + 0.5 * bandwidth * bandwidth * score
+
+
+def silverman_nd(data) -> float:
+    """Silverman rule with FP64 statistics (the reference's
+    experiments/error_suite_16d/reference.py:16-29 silverman_diag_bandwidth)."""
+    x = np.asarray(data, dtype=np.float64)
+    if x.ndim == 1:
+        x = x[:, None]
+    n, d = x.shape
+    sd = np.std(x, axis=0)
+    iqr = (np.percentile(x, 75, axis=0) - np.percentile(x, 25, axis=0)) / 1.34
+    sigma = float(np.mean(np.minimum(sd, iqr)))
+    if sigma <= 0:
+        sigma = 1.0
+    return float(0.9 * sigma * n ** (-1.0 / (d + 4)))
+
+
+def sdkde_1d(data) -> float:
+    x = np.asarray(data, dtype=np.float64).reshape(-1)
+    sd = float(x.std())
+    iqr = float(np.percentile(x, 75) - np.percentile(x, 25))
+    return 0.4 * min(sd, iqr / 1.34) * x.size ** (-1 / 9)

@@ -1,0 +1,77 @@
+"""The C-ABI library loads and exports every symbol include/fsk.h declares;
+argument checks happen on the host before any device work.  CPU only (no
+compute call reaches a GPU)."""
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+HEADERS = sorted((ROOT / "include").glob("*.h"))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from fsk import _build, _lib
+
+    _build.build()
+    return _lib.load()
+
+
+def declared_symbols():
+    names = []
+    for h in HEADERS:
+        names += re.findall(r"FSK_API\s+[\w\s\*]+?\b(fsk_\w+)\s*\(", h.read_text())
+    return sorted(set(names))
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    for required in ("fsk_kde16", "fsk_empscore16", "fsk_debias16", "fsk_kde1d", "fsk_kde1d_score",
+                     "fsk_silverman", "fsk_reduce_partials", "fsk_device_status", "fsk_strerror"):
+        assert required in names
+
+
+def test_every_declared_symbol_is_exported(lib):
+    from fsk import _lib
+
+    raw = ctypes.CDLL(str(_lib.LIB_PATH))
+    for name in declared_symbols():
+        assert hasattr(raw, name), name
+        assert name in _lib.SIGNATURES, f"{name} has no ctypes signature"
+
+
+def test_status_strings(lib):
+    from fsk import _lib as L
+
+    assert lib.fsk_version() >= 10000
+    for code in range(7):
+        assert L.strerror(code)
+    assert "timed out" in L.strerror(L.FSK_ERR_DEVICE_TIMEOUT)
+
+
+def test_argument_validation_is_host_side(lib):
+    from fsk import _lib as L
+
+    inval = L.FSK_ERR_INVALID_ARGUMENT
+    assert lib.fsk_kde16(None, 10, None, 10, 1.0, 0, 1.0, 0.0, None, None, 0, None) == inval
+    fake = ctypes.c_void_p(16)   # never dereferenced: the checks fail first
+    assert lib.fsk_kde16(fake, 0, fake, 10, 1.0, 0, 1.0, 0.0, fake, fake, 1 << 20, None) == inval
+    assert lib.fsk_kde16(fake, 10, fake, 10, -1.0, 0, 1.0, 0.0, fake, fake, 1 << 20, None) == inval
+    assert lib.fsk_kde16(fake, 10, fake, 10, float("inf"), 0, 1.0, 0.0, fake, fake, 1 << 20, None) == inval
+    assert lib.fsk_kde16(fake, 10, fake, 10, 1.0, 0x1000, 1.0, 0.0, fake, fake, 1 << 20, None) == inval
+    assert lib.fsk_empscore16(fake, 10, 1.0, 7, 0, fake, fake, fake, 1 << 20, None) == inval
+    assert lib.fsk_silverman(fake, 10, 65, 0, fake, fake, 1 << 20, None) == inval
+    assert lib.fsk_silverman(fake, 10, 2, 1, fake, fake, 1 << 20, None) == inval
+    assert lib.fsk_kde1d(fake, 10, fake, 0, 1.0, 0, 1.0, 0.0, fake, fake, 1 << 20, None) == inval
+    assert lib.fsk_reduce_partials(fake, 0, 10, fake, None) == inval
+
+
+def test_workspace_sizes(lib):
+    a = lib.fsk_kde16_workspace_bytes(1 << 10, 1 << 12, 0)
+    b = lib.fsk_kde16_workspace_bytes(1 << 20, 1 << 20, 0)
+    assert 0 < a < b
+    assert lib.fsk_kde16_workspace_bytes(0, 10, 0) == 0
+    assert lib.fsk_empscore16_workspace_bytes(1 << 16, 0, 0) > (1 << 16) * 17 * 8
+    assert lib.fsk_silverman_workspace_bytes(100, 16) > 0

@@ -1,0 +1,108 @@
+"""Host-side logic of the drop-in API that needs no GPU: validation order and
+exception types (ValueError for bad arguments, as in the reference),
+backend/precision validators, split heuristics and workload generators."""
+import numpy as np
+import pytest
+
+
+def test_validators():
+    from flash_sd_kde import config as C
+
+    C.validate_precision_mode("fast_tf32")
+    C.validate_precision_mode("fp32_ieee")
+    with pytest.raises(ValueError):
+        C.validate_precision_mode("bf16")
+    with pytest.raises(ValueError):
+        C.validate_kde_backend("nope")
+    with pytest.raises(ValueError):
+        C.validate_emp_score_backend("nope")
+    assert C.select_emp_score_backend(10) == "flash_sd_kde"
+    h = C.KernelHeuristics(default_emp_score_backend="ordered_splitk")
+    assert C.select_emp_score_backend(10, heuristics=h) == "symmetric_atomic"
+    assert C.select_emp_score_backend(10**6, heuristics=h) == "ordered_splitk"
+    assert C.compute_splitk_splits(4096, block_n_iter=128, iters_per_split=8) == 4
+    assert C.cap_splits_for_memory(1 << 22, 4096, features=16) == 1
+    assert C.cap_splits_for_memory(1000, 7, features=16) == 7
+
+
+def test_kde_eval_rejects_bad_arguments_before_device_work():
+    from flash_sd_kde import emp_sd_kde_fit_transform, kde_eval
+
+    x = np.zeros((8, 16), np.float32)
+    with pytest.raises(ValueError):
+        kde_eval(x, x, 0.0)
+    with pytest.raises(ValueError):
+        kde_eval(x, x, 1.0, device="cpu")
+    with pytest.raises(ValueError):
+        kde_eval(x, x, 1.0, precision_mode="tf64")
+    with pytest.raises(ValueError):
+        kde_eval(x, x, 1.0, kde_backend="bogus")
+    with pytest.raises(ValueError):
+        emp_sd_kde_fit_transform(x, -1.0)
+    with pytest.raises(ValueError):
+        emp_sd_kde_fit_transform(x, 1.0, emp_score_backend="bogus")
+    with pytest.raises(ValueError):
+        emp_sd_kde_fit_transform(x, 1.0, device="cpu")
+
+
+def test_estimator_input_validation():
+    from flash_sd_kde import FlashSDKDE
+
+    est = FlashSDKDE()
+    with pytest.raises(ValueError):
+        est._validate_input(np.zeros(5, np.float32))
+    with pytest.raises(ValueError):
+        est._validate_input(np.zeros((0, 16), np.float32))
+    with pytest.raises(ValueError):
+        est._validate_input(np.zeros((3, 0), np.float32))
+    with pytest.raises(ValueError):
+        FlashSDKDE(mode="bogus")._validate_mode()
+    with pytest.raises(ValueError):
+        est.score_samples(np.zeros((3, 16), np.float32))
+
+
+def test_kernel_wrappers_reject_bad_arguments():
+    from kernels.flash_sd_kde import gaussian_kde_triton_nd, emp_score_16d_flash_sd_kde
+    from kernels.kde_eval_16d_stream_splitk import kde_eval_16d_splitk
+
+    x = np.zeros((4, 16), np.float32)
+    with pytest.raises(ValueError):
+        gaussian_kde_triton_nd(x, x, 0.0)
+    with pytest.raises(ValueError):
+        gaussian_kde_triton_nd(x, x, 1.0, device="cpu")
+    with pytest.raises(ValueError):
+        emp_score_16d_flash_sd_kde(x, 1.0, device="cpu")
+    with pytest.raises(ValueError):
+        kde_eval_16d_splitk(x, x, -2.0, device="cuda", precision_mode="fast_tf32",
+                            use_precomputed_norms=True, autotune=False)
+
+
+def test_workloads_are_seeded_and_shaped():
+    from fsk import workloads as W
+
+    a, b = W.plain_kde_16d()
+    assert a.shape == (4096, 16) and b.shape == (1024, 16) and a.dtype == np.float32
+    a2, _ = W.plain_kde_16d()
+    assert np.array_equal(a, a2)
+    g = W.GMM16(seed=0)
+    assert np.isclose(g.weights.sum(), 1.0) and g.cov.shape == (8, 16, 16)
+    s = g.sample(1000, seed=1)
+    assert s.shape == (1000, 16) and np.isfinite(g.log_density(s)).all()
+    t = W.student_t_16d(1000, seed=4)
+    assert abs(np.median(t) - 100) < 5
+    lr = W.lowrank_16d(10000)
+    assert np.allclose(lr.std(0), np.arange(1, 17) ** -0.5, rtol=0.05)
+    x1 = W.gmm3_1d(10000)
+    assert x1.shape == (10000,)
+    grid = W.grid_1d(11)
+    assert grid[0] == -5 and grid[-1] == 6
+
+
+def test_shard_partition_covers_rows():
+    from fsk.workloads import shard
+
+    for count in (1, 7, 1000, 1 << 20):
+        for world in (1, 2, 3, 8):
+            spans = [shard(count, world, r) for r in range(world)]
+            assert spans[0][0] == 0 and spans[-1][1] == count
+            assert all(spans[i][1] == spans[i + 1][0] for i in range(world - 1))

@@ -1,0 +1,169 @@
+"""16-D KDE through the C ABI on the GPU, both precision modes, against the
+reference's own outputs (golden fixtures) and the FP64 oracle.
+
+Tolerances (relative, on densities unless stated):
+  * vs the reference FP32 CPU path: 1e-5 (the bar of the target spec);
+  * vs the FP64 oracle: max 1e-5, median 1e-6;
+  * relative log-density error vs FP64: 1e-6 (spec bar 1e-5).
+"""
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_err
+from oracle import fp64
+from oracle import reference_numpy as R
+
+pytestmark = pytest.mark.gpu
+PRECISIONS = ["tensor", "ieee"]
+
+
+def _kde(dev, q, x, h, precision="tensor", **kw):
+    from fsk import ops
+
+    norm = 1.0 / ((2.0 * np.pi) ** 8 * h ** 16 * x.shape[0])
+    out = ops.kde16_sum(torch.from_numpy(np.ascontiguousarray(q)).to(dev),
+                        torch.from_numpy(np.ascontiguousarray(x)).to(dev), h, precision=precision,
+                        out_scale=kw.pop("scale", norm), **kw)
+    ops.device_status(dev)
+    return out.cpu().numpy().astype(np.float64)
+
+
+def test_mma_probe_layout(cuda_dev):
+    """Two K=16 tcgen05.mma steps (fp16, M=128, N=64) over the 64-byte-row
+    operand images of the KDE kernel equal the host dot product of the
+    fp16-rounded operands: pins the smem/instruction descriptors, the K-step
+    offset and the TMEM lane/column mapping."""
+    from fsk import ops
+
+    g = torch.Generator().manual_seed(0)
+    a = torch.randn(128, 32, generator=g) * 3
+    b = torch.randn(64, 32, generator=g) * 3
+    d = ops.mma_probe(a.to(cuda_dev), b.to(cuda_dev)).cpu().double()
+    ah, bh = a.half().double(), b.half().double()
+    ref = ah @ bh.T
+    scale = ah.abs() @ bh.abs().T
+    assert ((d - ref).abs() <= 2e-6 * scale + 1e-30).all(), float(((d - ref).abs() / scale).max())
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_plain_4096x1024_vs_reference_and_fp64(cuda_dev, golden, precision):
+    g = golden("kde16_plain_4096x1024")
+    out = _kde(cuda_dev, g["queries"], g["train"], float(g["h"]), precision)
+    truth = np.exp(g["log_density_fp64"])
+    e64 = rel_err(out, truth)
+    assert e64.max() < 1e-5 and np.median(e64) < 1e-6, (e64.max(), np.median(e64))
+    assert rel_err(out, g["density"]).max() < 1e-5
+    rel_log = np.abs(np.log(out) - g["log_density_fp64"]) / np.abs(g["log_density_fp64"])
+    assert rel_log.max() < 1e-6
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("name", ["kde16_seed1", "kde16_seed11"])
+def test_reference_test_cases(cuda_dev, golden, precision, name):
+    g = golden(name)
+    out = _kde(cuda_dev, g["queries"], g["train"], float(g["h"]), precision)
+    assert rel_err(out, g["density"]).max() < 1e-5
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("name", ["kde16_lin_seed5", "kde16_lin_seed7"])
+def test_laplace_reference_cases(cuda_dev, golden, precision, name):
+    g = golden(name)
+    out = _kde(cuda_dev, g["queries"], g["train"], float(g["h"]), precision, laplace=True)
+    ref = g["density"].astype(np.float64)
+    np.testing.assert_allclose(out, ref, rtol=1e-5, atol=1e-5 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("m,n", [(1, 1), (1, 300), (129, 1), (100, 127), (257, 129), (255, 4097), (513, 1000)])
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_ragged_and_tiny_shapes(cuda_dev, m, n, precision):
+    rng = np.random.default_rng(m * 7919 + n)
+    x = rng.standard_normal((n, 16)).astype(np.float32)
+    q = (rng.standard_normal((m, 16)) * 0.8).astype(np.float32)
+    h = 0.9
+    out = _kde(cuda_dev, q, x, h, precision)
+    truth = fp64.density(x, q, h)
+    assert rel_err(out, truth).max() < 1e-5
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_offset_heavy_tail_cancellation(cuda_dev, precision):
+    """Student-t data with a +100 offset: the norm expansion cancels
+    catastrophically in FP32 without centring (the reference's FP32 path is
+    off by up to 100% here); the kernels must stay at FP64-level accuracy."""
+    from fsk import workloads
+
+    x = workloads.student_t_16d(8192, seed=4)
+    q = workloads.student_t_16d(512, seed=5)
+    h0 = R.silverman_bandwidth_nd(x)
+    for f in (0.5, 1.0, 2.0):
+        h = h0 * f
+        from fsk import ops
+
+        lp = ops.kde16_sum(torch.from_numpy(q).to(cuda_dev), torch.from_numpy(x).to(cuda_dev), h,
+                           precision=precision, out_scale=1.0 / ((2 * np.pi) ** 8 * h ** 16 * x.shape[0]),
+                           log_eps=0.0).cpu().numpy().astype(np.float64)
+        ref = fp64.log_density(x, q, h)
+        ok = np.isfinite(ref) & (ref > -80.0)      # densities representable in FP32
+        rel_log = np.abs(lp[ok] - ref[ok]) / np.abs(ref[ok])
+        assert rel_log.max() < 1e-6, (f, rel_log.max())
+
+
+def test_tensor_path_is_deterministic_and_atomic_agrees(cuda_dev, golden):
+    g = golden("kde16_plain_4096x1024")
+    a = _kde(cuda_dev, g["queries"], g["train"], float(g["h"]))
+    b = _kde(cuda_dev, g["queries"], g["train"], float(g["h"]))
+    assert np.array_equal(a, b)
+    c = _kde(cuda_dev, g["queries"], g["train"], float(g["h"]), atomic=True)
+    assert rel_err(c, a).max() < 1e-6
+
+
+def test_query_chunking_invariance(cuda_dev, golden):
+    """tests/large/test_consistency_large.py:59-73 of the reference."""
+    g = golden("kde16_seed11")
+    full = _kde(cuda_dev, g["queries"], g["train"], float(g["h"]))
+    half = g["queries"].shape[0] // 2
+    a = _kde(cuda_dev, g["queries"][:half], g["train"], float(g["h"]))
+    b = _kde(cuda_dev, g["queries"][half:], g["train"], float(g["h"]))
+    assert rel_err(np.concatenate([a, b]), full).max() < 1e-7
+
+
+def test_log_output_matches(cuda_dev, golden):
+    g = golden("kde16_plain_4096x1024")
+    d = _kde(cuda_dev, g["queries"], g["train"], float(g["h"]))
+    h = float(g["h"])
+    lp = _kde(cuda_dev, g["queries"], g["train"], h, log_eps=1e-12)
+    np.testing.assert_allclose(lp, np.log(d + 1e-12), rtol=1e-6)
+
+
+def test_invalid_arguments_raise_value_error(cuda_dev):
+    from fsk import ops
+
+    x = torch.zeros(10, 16, device=cuda_dev)
+    with pytest.raises(ValueError):
+        ops.kde16_sum(x, x, 0.0)
+    with pytest.raises(ValueError):
+        ops.kde16_sum(x, x, float("nan"))
+    with pytest.raises(ValueError):
+        ops.kde16_sum(torch.zeros(10, 15, device=cuda_dev), x, 1.0)
+    with pytest.raises(ValueError):
+        ops.kde16_sum(torch.zeros(0, 16, device=cuda_dev), x, 1.0)
+
+
+def test_bounded_wait_timeout_is_reported(cuda_dev):
+    """A kernel waits on an mbarrier nothing arrives on; the wait gives up
+    (~2 s), the status is read on the host and the context stays usable."""
+    from fsk import _lib as L
+    from fsk import ops
+
+    flag = torch.full((1,), -1, dtype=torch.int32, device=cuda_dev)
+    st = L.load().fsk_diag_wait_timeout_probe(flag.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    assert st == L.FSK_OK
+    with pytest.raises(L.FskError) as ei:
+        ops.device_status(cuda_dev)
+    assert ei.value.status == L.FSK_ERR_DEVICE_TIMEOUT
+    assert int(flag.item()) == 0
+    ops.device_status(cuda_dev)          # cleared
+    x = torch.randn(64, 16, device=cuda_dev)
+    assert torch.isfinite(ops.kde16_sum(x, x, 1.0)).all()

@@ -1,0 +1,71 @@
+"""The oracle restatement pinned against fixtures produced by the reference's
+own CPU code (tests/golden/make_golden.py).  CPU only."""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from oracle import fp64
+from oracle import reference_numpy as R
+
+
+@pytest.mark.parametrize("name", ["kde16_seed1", "kde16_seed11", "kde16_plain_4096x1024"])
+def test_kde_nd_matches_reference(golden, name):
+    g = golden(name)
+    out = R.kde_eval_nd_numpy(g["queries"], g["train"], float(g["h"]))
+    assert rel_err(out, g["density"]).max() < 2e-6
+
+
+@pytest.mark.parametrize("name", ["kde16_lin_seed5", "kde16_lin_seed7"])
+def test_kde_nd_linearized_matches_reference(golden, name):
+    g = golden(name)
+    out = R.kde_eval_nd_linearized_numpy(g["queries"], g["train"], float(g["h"]))
+    np.testing.assert_allclose(out, g["density"], rtol=2e-6, atol=1e-12)
+
+
+def test_kde_1d_matches_reference(golden):
+    g = golden("kde1d_seed0")
+    np.testing.assert_allclose(R.kde_eval_1d_numpy(g["queries"], g["train"], float(g["h"])), g["density"], rtol=1e-6)
+    g = golden("kde1d_lin_seed6")
+    np.testing.assert_allclose(R.kde_eval_1d_numpy(g["queries"], g["train"], float(g["h"]), laplace=True),
+                               g["density"], rtol=1e-6, atol=1e-9)
+
+
+@pytest.mark.parametrize("seed", [2, 3, 4, 10])
+def test_empirical_score_matches_reference(golden, seed):
+    g = golden(f"score16_seed{seed}")
+    pdf, w, score = R.empirical_score_nd_numpy(g["train"], float(g["h"]))
+    np.testing.assert_allclose(pdf, g["pdf_sum"], rtol=2e-6)
+    np.testing.assert_allclose(w, g["weighted"], rtol=2e-5, atol=2e-5)
+    deb = R.empirical_sd_kde_transform_nd_numpy(g["train"], float(g["h"]))
+    np.testing.assert_allclose(deb, g["debiased"], rtol=1e-5, atol=1e-5)
+
+
+def test_silverman_matches_reference(golden):
+    g = golden("kde16_plain_4096x1024")
+    assert R.silverman_bandwidth_nd(g["train"]) == pytest.approx(float(g["h"]), rel=1e-12)
+    s = golden("silverman_seed13")
+    assert R.silverman_bandwidth_nd(s["data"]) == pytest.approx(float(s["h_nd"]), rel=1e-12)
+    assert R.silverman_bandwidth(s["data"][:, 3]) == pytest.approx(float(s["h_1d"]), rel=1e-12)
+    assert fp64.silverman_nd(g["train"]) == pytest.approx(float(g["silverman_fp64"]), rel=1e-12)
+
+
+def test_kde_score_1d_matches_reference(golden):
+    g = golden("kde1d_score_seed12")
+    score, pdf, _ = R.kde_score_1d(g["queries"], g["train"], float(g["h"]))
+    np.testing.assert_allclose(pdf, g["pdf"], rtol=1e-5)
+    np.testing.assert_allclose(score, g["score"], rtol=1e-4, atol=1e-4)
+    assert R.sdkde_1d_bandwidth(g["mixture"]) == pytest.approx(float(g["h_sdkde"]), rel=1e-6)
+
+
+def test_fp64_oracle_matches_reference_fp64(golden):
+    g = golden("kde16_plain_4096x1024")
+    lp = fp64.log_density(g["train"], g["queries"], float(g["h"]))
+    np.testing.assert_allclose(lp, g["log_density_fp64"], rtol=1e-12, atol=1e-10)
+    # and the reference's FP32 path is within 1e-5 of it (documented oracle fidelity)
+    assert rel_err(g["density"], np.exp(g["log_density_fp64"])).max() < 1e-5
+
+
+def test_fp64_laplace_matches_fp32_oracle(golden):
+    g = golden("kde16_lin_seed5")
+    d64 = fp64.density(g["train"], g["queries"], float(g["h"]), laplace=True)
+    np.testing.assert_allclose(d64, np.abs(g["density"]), rtol=1e-4)
