@@ -46,6 +46,7 @@ _int = _c.c_int
 SIGNATURES: dict[str, tuple] = {
     "fsk_kde16_workspace_bytes": (_sz, [_i64, _i64, _int]),
     "fsk_kde16": (_int, [_vp, _i64, _vp, _i64, _d, _int, _d, _d, _vp, _vp, _sz, _vp]),
+    "fsk_kde16_noalloc": (_int, [_vp, _i64, _vp, _i64, _d, _int, _d, _d, _vp, _vp]),
     "fsk_empscore16_workspace_bytes": (_sz, [_i64, _int, _int]),
     "fsk_empscore16": (_int, [_vp, _i64, _d, _int, _int, _vp, _vp, _vp, _sz, _vp]),
     "fsk_debias16": (_int, [_vp, _i64, _vp, _vp, _i64, _i64, _d, _d, _vp, _vp, _vp]),

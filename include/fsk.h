@@ -98,6 +98,22 @@ FSK_API int fsk_kde16(const float* queries, int64_t m, const float* data, int64_
               double bandwidth, int flags, double out_scale, double out_eps,
               float* out, void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---- 16-D Gaussian KDE without a caller workspace ------------------------ */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory (C-ABI/FFI hosts without a device allocator of their own, processes
+ * whose GPU memory another allocator owns, loops where cudaMalloc/cudaFree
+ * would synchronise the device): same arguments and result as fsk_kde16,
+ * with the scratch in a fixed device array of FSK_NOALLOC_SCRATCH_BYTES held
+ * by every GPU that loads the library.  Requests needing more
+ * (fsk_kde16_workspace_bytes) fail with FSK_ERR_SCRATCH_LIMIT.  All calls
+ * share the array: calls whose GPU work overlaps race and must be
+ * serialised.  The first call on a device looks up the array's address;
+ * make it before any stream capture.  Allocates nothing. */
+#define FSK_NOALLOC_SCRATCH_BYTES (32u << 20)
+FSK_API int fsk_kde16_noalloc(const float* queries, int64_t m, const float* data, int64_t n,
+                              double bandwidth, int flags, double out_scale, double out_eps,
+                              float* out, void* stream);
+
 /* ---- 16-D empirical-score accumulators --------------------------------- */
 /* pdf_sum[i] = sum_j phi_ij, weighted_sum[i,:] = sum_j phi_ij x_j, the
  * self-pair included (flash_sd_kde/reference.py:263-284). */
