@@ -21,11 +21,14 @@
 //    kind::f16, M=128, N=64, FP32 accumulation in tensor memory) *is* a2.
 //  * Epilogue: tcgen05.ld one query row per thread, 2^D on the SFU
 //    (ex2.approx), 32-column chunk sums, compensated (TwoSum) per query.
-//  * Exact near-pair recompute: every term above 2^-8 of its query's running
-//    sum (including the current chunk) is recomputed from direct FP32
-//    differences of the original coordinates with the exponent product in
-//    double-float.  Terms never recomputed are each below 2^-8 of the final
-//    sum and carry the ~2^-21 relative error of the fp16x3 product.
+//  * Exact near-pair recompute: when a 32-column chunk holds more than 1/64
+//    of its query's running sum (carried across the data splits a CTA runs
+//    for that query block), the chunk's largest term is recomputed from
+//    direct FP32 differences of the original coordinates with the exponent
+//    product in double-float, and replaces its approximation.  The argmax
+//    rides in the low 5 mantissa bits, so all triggered lanes of a warp
+//    recompute one pair each in lock-step.  Other terms carry the ~2^-21
+//    relative error of the fp16x3 product, which averages out.
 //
 // Pipeline (one persistent CTA per SM, 18 warps):
 //   warp 16 : producer - bulk (TMA) copies of query images per unit and of
@@ -38,33 +41,10 @@
 
 #include "fsk_kernels.cuh"
 #include "fsk_tc.cuh"
+#include "fsk_tc_ops.cuh"
 
 namespace fsk {
 namespace tc {
-
-// ---- idesc / descriptors for fp16 operands ---------------------------------------
-__host__ __device__ constexpr uint32_t idesc_f16_f32(int M, int N) {
-  return (1u << 4)                      // D format F32
-         | (0u << 7) | (0u << 10)       // A, B format F16
-         | (uint32_t(N >> 3) << 17) | (uint32_t(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_f16_ss(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc,
-                                           uint32_t idesc, uint32_t accumulate) {
-  mma_bf16_ss(d_tmem, a_desc, b_desc, idesc, accumulate);  // same instruction, kind::f16
-}
-
-// sum_k (q_k - x_k)^2 from the original FP32 coordinates of data row r.
-__device__ __forceinline__ float exact_dist(const uint8_t* stage, int r, const float (&q)[FSK_D]) {
-  const float4* xr = reinterpret_cast<const float4*>(stage + B_X_OFFSET + r * (FSK_D * 4));
-  float xv[FSK_D];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const float4 v = xr[k];
-    xv[4 * k] = v.x; xv[4 * k + 1] = v.y; xv[4 * k + 2] = v.z; xv[4 * k + 3] = v.w;
-  }
-  return sqdist16(q, xv);
-}
 
 template <bool LAPLACE>
 __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
@@ -104,13 +84,18 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
+  // Work units are (query block, data split), query-block-major; each CTA
+  // takes one contiguous range of units so consecutive splits of a query
+  // block run back to back and the epilogue can carry its running sums.
   const int64_t units = p.q_blocks * p.splits;
+  const int64_t u_begin = (int64_t)blockIdx.x * units / gridDim.x;
+  const int64_t u_end = (int64_t)(blockIdx.x + 1) * units / gridDim.x;
 
   if (warp == PRODUCER_WARP) {
     if (lane == 0) {
       int64_t g = 0, k = 0;
-      for (int64_t u = blockIdx.x; u < units; u += gridDim.x, ++k) {
-        const int64_t qb = u % p.q_blocks, sp = u / p.q_blocks;
+      for (int64_t u = u_begin; u < u_end; ++u, ++k) {
+        const int64_t qb = u / p.splits, sp = u % p.splits;
         if (!mbar_wait(qempty, (uint32_t)((k & 1) ^ 1), 1)) goto done;
         mbar_arrive_expect_tx(qready, A_BYTES);
         bulk_g2s(sA, p.qimg + qb * (int64_t)A_BYTES, A_BYTES, qready);
@@ -128,8 +113,8 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
     if (lane == 0) {
       const uint32_t idesc = idesc_f16_f32(QT, NT);
       int64_t g = 0, k = 0;
-      for (int64_t u = blockIdx.x; u < units; u += gridDim.x, ++k) {
-        const int64_t sp = u / p.q_blocks;
+      for (int64_t u = u_begin; u < u_end; ++u, ++k) {
+        const int64_t sp = u % p.splits;
         if (!mbar_wait(qready, (uint32_t)(k & 1), 3)) goto done;
         const int64_t t0 = sp * p.tiles_per_split;
         const int64_t t1 = imin<int64_t>(p.n_tiles, t0 + p.tiles_per_split);
@@ -170,8 +155,14 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
     const float out_mul = p.scales->out_mul;
     const bool scaled = out_mul != 1.0f;
     int64_t g = 0;
-    for (int64_t u = blockIdx.x; u < units; u += gridDim.x) {
-      const int64_t qb = u % p.q_blocks, sp = u / p.q_blocks;
+    int64_t prev_qb = -1;
+    float s_carry = 0.f;   // approximate sum of this query over the splits already done here
+    for (int64_t u = u_begin; u < u_end; ++u) {
+      const int64_t qb = u / p.splits, sp = u % p.splits;
+      if (qb != prev_qb) {
+        s_carry = 0.f;
+        prev_qb = qb;
+      }
       const int64_t gi = qb * (NQT * QT) + qt * QT + row;   // padded query index
       float qx[FSK_D];
 #pragma unroll
@@ -209,64 +200,80 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
 #pragma unroll
             for (int j = 0; j < 32; ++j) e[j] = __uint_as_float(r[j]);
           }
-          float ps0 = 0.f, ps1 = 0.f, ps2 = 0.f, ps3 = 0.f;
 #pragma unroll
-          for (int j = 0; j < 32; j += 4) {
-            float v0 = ex2_approx(e[j]), v1 = ex2_approx(e[j + 1]);
-            float v2 = ex2_approx(e[j + 2]), v3 = ex2_approx(e[j + 3]);
-            if (LAPLACE) {
-              // 1 + d/2 - dist/(2h^2) = 9 + a2 ln 2   (a2 = -c2 dist)
-              v0 *= fmaf(e[j], 0.69314718055994531f, 1.0f + 0.5f * FSK_D);
-              v1 *= fmaf(e[j + 1], 0.69314718055994531f, 1.0f + 0.5f * FSK_D);
-              v2 *= fmaf(e[j + 2], 0.69314718055994531f, 1.0f + 0.5f * FSK_D);
-              v3 *= fmaf(e[j + 3], 0.69314718055994531f, 1.0f + 0.5f * FSK_D);
-            }
-            e[j] = v0; e[j + 1] = v1; e[j + 2] = v2; e[j + 3] = v3;
+          for (int j = 0; j < 32; ++j) {
+            float v = ex2_approx(e[j]);
+            // Laplace factor 1 + d/2 - dist/(2h^2) = 9 + a2 ln 2   (a2 = -c2 dist)
+            if (LAPLACE) v *= fmaf(e[j], 0.69314718055994531f, 1.0f + 0.5f * FSK_D);
+            e[j] = v;
           }
           if (valid < NT) {  // ragged last data tile: drop padding columns
 #pragma unroll
             for (int j = 0; j < 32; ++j)
               if (c * 32 + j >= valid) e[j] = 0.f;
           }
+          // packed pairwise sum (f32x2 adds on register pairs)
+          float2 pa = make_float2(e[0], e[1]), pb = make_float2(e[2], e[3]);
 #pragma unroll
-          for (int j = 0; j < 32; j += 4) {
-            ps0 += e[j]; ps1 += e[j + 1]; ps2 += e[j + 2]; ps3 += e[j + 3];
+          for (int j = 4; j < 32; j += 4) {
+            pa = __fadd2_rn(pa, make_float2(e[j], e[j + 1]));
+            pb = __fadd2_rn(pb, make_float2(e[j + 2], e[j + 3]));
           }
-          const float cs = (ps0 + ps1) + (ps2 + ps3);
-          const float thr = (fabsf(acc.s) + fabsf(cs)) * NEAR_FRACTION;
-          bool scan = false;
+          pa = __fadd2_rn(pa, pb);
+          float cs = pa.x + pa.y;
+          // Near-pair test: a chunk holding more than NEAR_FRACTION of the
+          // running sum (this chunk included) may contain a dominant term.
+          const bool trig = fabsf(cs) > (s_carry + fabsf(acc.s) + fabsf(cs)) * NEAR_FRACTION;
+          if (__any_sync(0xffffffffu, trig)) {
+            // Triggered lanes replace their chunk's largest term by its exact
+            // value.  The argmax rides in the low 5 mantissa bits of each term
+            // (key = |e| with bits[4:0] := column); the chunk is re-summed
+            // from those keyed values, so subtracting the keyed maximum
+            // removes exactly what was added.  All triggered lanes recompute
+            // one pair each, in lock-step.
+            if (trig) {
+              uint32_t key[32];
+              float2 qa = make_float2(0.f, 0.f), qb = make_float2(0.f, 0.f);
 #pragma unroll
-          for (int j = 0; j < 32; j += 8) {
-            const float m01 = fmaxf(fabsf(e[j]), fabsf(e[j + 1])), m23 = fmaxf(fabsf(e[j + 2]), fabsf(e[j + 3]));
-            const float m45 = fmaxf(fabsf(e[j + 4]), fabsf(e[j + 5])), m67 = fmaxf(fabsf(e[j + 6]), fabsf(e[j + 7]));
-            scan |= fmaxf(fmaxf(m01, m23), fmaxf(m45, m67)) > thr;
-          }
-          if (scan) {
-            // rare path: every term above the threshold is recomputed exactly
-            uint32_t mask = 0u;
-            float approx_near = 0.f;
+              for (int j = 0; j < 32; j += 2) {
+                // terms are >= 0 except with the Laplace factor
+                const float a0 = LAPLACE ? fabsf(e[j]) : e[j], a1 = LAPLACE ? fabsf(e[j + 1]) : e[j + 1];
+                key[j] = (__float_as_uint(a0) & ~31u) | (uint32_t)j;
+                key[j + 1] = (__float_as_uint(a1) & ~31u) | (uint32_t)(j + 1);
+                const float v0 = LAPLACE ? copysignf(__uint_as_float(key[j]), e[j]) : __uint_as_float(key[j]);
+                const float v1 = LAPLACE ? copysignf(__uint_as_float(key[j + 1]), e[j + 1]) : __uint_as_float(key[j + 1]);
+                if (j & 2) qb = __fadd2_rn(qb, make_float2(v0, v1));
+                else qa = __fadd2_rn(qa, make_float2(v0, v1));
+              }
+              // max tree over the keys
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
-              const bool nr = fabsf(e[j]) > thr;
-              mask |= (nr ? 1u : 0u) << j;
-              approx_near += nr ? e[j] : 0.f;
-            }
-            corr -= approx_near;
-            while (mask) {
-              const int j = __ffs(mask) - 1;
-              mask &= mask - 1u;
+              for (int w = 16; w >= 1; w >>= 1)
+#pragma unroll
+                for (int j = 0; j < w; ++j) key[j] = max(key[j], key[j + w]);
+              const uint32_t kmax = key[0];
+              qa = __fadd2_rn(qa, qb);
+              cs = qa.x + qa.y;
+              const int j = (int)(kmax & 31u);
+              float approx = __uint_as_float(kmax);
+              if (LAPLACE) {
+#pragma unroll
+                for (int jj = 0; jj < 32; ++jj)
+                  if (jj == j) approx = copysignf(approx, e[jj]);
+              }
               const float dist = exact_dist(stage, c * 32 + j, qx);
               float ex = exp2_neg_scaled(dist, p.c2, p.c2_lo);
               if (LAPLACE) ex *= fmaf(-p.c1, dist, 1.0f + 0.5f * FSK_D);
-              corr += ex;
+              if (c * 32 + j >= valid) ex = 0.f;
+              corr += ex - approx;
             }
+            __syncwarp();
           }
-          __syncwarp();
           acc.add(cs);
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[s]);
       }
+      s_carry += fabsf(acc.s + corr);
       if (gi < p.m) {
         const double v = (double)acc.s + (double)acc.c + (double)corr;
         if (p.atomic_acc) atomicAdd(&p.atomic_acc[gi], v);
@@ -282,10 +289,6 @@ done:
 }
 
 // ---- prep ----------------------------------------------------------------------------
-__device__ __forceinline__ void atomic_max_pos(unsigned int* addr, float v) {
-  atomicMax(addr, __float_as_uint(fmaxf(v, 0.f)));  // non-negative floats order as integers
-}
-
 // Maxima for the scale selection: |2 c2 (q-mu)|, c2 |q-mu|^2 over queries and
 // |x-mu|, c2 |x-mu|^2 over data.  One thread per row; block-reduced.
 __global__ void scale_stats_kernel(const float* __restrict__ pts, int64_t count, const float* __restrict__ mu,
@@ -352,46 +355,6 @@ __global__ void scale_select_kernel(TcScales* sc) {
   sc->out_mul = ldexpf(1.f, es);
 }
 
-// Splits v into three fp16 parts (hi, mid, lo) that sum to v to ~33 bits.
-__device__ __forceinline__ void split3_f16(float v, __half& a, __half& b, __half& c) {
-  a = __float2half_rn(v);
-  const float r1 = v - __half2float(a);
-  b = __float2half_rn(r1);
-  c = __float2half_rn(r1 - __half2float(b));
-}
-
-__device__ __forceinline__ void put_h(uint8_t* img, int r, int k, int row_bytes, __half v) {
-  *reinterpret_cast<__half*>(img + cm_offset(r, k, row_bytes)) = v;
-}
-
-// Writes one operand row: H image (features hi + 16 bias columns) and L
-// image (features lo).  bias_own: three parts of this row's own norm term;
-// pow_other: the exact power of two multiplying the other side's parts.
-__device__ __forceinline__ void write_operand_row(uint8_t* h_img, uint8_t* l_img, int r, const float (&v)[FSK_D],
-                                                  float own_term, float pow_other, bool own_first) {
-#pragma unroll
-  for (int k = 0; k < FSK_D; ++k) {
-    const __half hi = __float2half_rn(v[k]);
-    const __half lo = __float2half_rn(v[k] - __half2float(hi));
-    put_h(h_img, r, k, H_ROW_BYTES, hi);
-    put_h(l_img, r, k, L_ROW_BYTES, lo);
-  }
-  __half p0, p1, p2;
-  split3_f16(own_term, p0, p1, p2);
-  const __half one = __float2half_rn(pow_other);
-  const __half zero = __float2half_rn(0.f);
-  // bias columns 16..21: A = [2^eb x3 | alpha parts x3], B = [beta parts x3 | 2^ea x3]
-  const int own = own_first ? 16 : 19, oth = own_first ? 19 : 16;
-  put_h(h_img, r, own + 0, H_ROW_BYTES, p0);
-  put_h(h_img, r, own + 1, H_ROW_BYTES, p1);
-  put_h(h_img, r, own + 2, H_ROW_BYTES, p2);
-  put_h(h_img, r, oth + 0, H_ROW_BYTES, one);
-  put_h(h_img, r, oth + 1, H_ROW_BYTES, one);
-  put_h(h_img, r, oth + 2, H_ROW_BYTES, one);
-#pragma unroll
-  for (int k = 22; k < KH; ++k) put_h(h_img, r, k, H_ROW_BYTES, zero);
-}
-
 // data tile image: [H (NT x 32 fp16) | L (NT x 16 fp16) | x (NT x 16 FP32)]
 __global__ void prep_data_kernel(const float* __restrict__ x, int64_t n, int64_t n_pad,
                                  const float* __restrict__ mu, float c2, const TcScales* __restrict__ sc,
@@ -448,15 +411,26 @@ TcPlan plan_kde16(int64_t m, int64_t n) {
   pl.n_tiles = (n + NT - 1) / NT;
   pl.n_pad = pl.n_tiles * NT;
   pl.q_blocks = pl.m_pad / (NQT * QT);
-  const int sms = sm_count();
-  // splits: keep a split's data image around 16 MB (L2-resident while every
-  // query block streams it) and give every SM several units.
-  const int64_t l2_tiles = (16ll << 20) / B_STAGE_BYTES;
-  int64_t splits = (pl.n_tiles + l2_tiles - 1) / l2_tiles;
-  const int64_t want_units = 4ll * sms;
-  if (pl.q_blocks * splits < want_units) splits = (want_units + pl.q_blocks - 1) / pl.q_blocks;
-  splits = imax<int64_t>(1, imin<int64_t>(splits, pl.n_tiles));
-  pl.tiles_per_split = (pl.n_tiles + splits - 1) / splits;
+  const int64_t sms = sm_count();
+  // Data splits only add parallelism: pick the smallest split count giving
+  // every CTA >= 4 units with a near-integral number of units per CTA.
+  const int64_t s_min = imax<int64_t>(1, imin<int64_t>(pl.n_tiles, (4 * sms + pl.q_blocks - 1) / pl.q_blocks));
+  const int64_t s_max = imin<int64_t>(pl.n_tiles, 4 * s_min + 16);
+  int64_t best = s_min;
+  double best_eff = -1.0;
+  for (int64_t sp = s_min; sp <= s_max; ++sp) {
+    const int64_t tps = (pl.n_tiles + sp - 1) / sp;
+    const int64_t eff_splits = (pl.n_tiles + tps - 1) / tps;
+    const int64_t u = pl.q_blocks * eff_splits;
+    const int64_t g = imin<int64_t>(u, sms);
+    const double eff = (double)u / (double)(g * ((u + g - 1) / g));
+    if (eff > best_eff + 1e-9) {
+      best_eff = eff;
+      best = sp;
+    }
+    if (eff >= 0.97) break;
+  }
+  pl.tiles_per_split = (pl.n_tiles + best - 1) / best;
   pl.splits = (pl.n_tiles + pl.tiles_per_split - 1) / pl.tiles_per_split;  // all splits non-empty
   pl.grid = (int)imin<int64_t>(pl.q_blocks * pl.splits, sms);
   return pl;
