@@ -48,7 +48,7 @@ C_OPS_PER_PAIR = 3.0
 K_OPS_PER_POLY_EXP = 10.0
 KERNEL_NAMES = {1: "kde16_tc_kernel", 2: "kde16_simt_kernel", 3: "score16_simt_kernel",
                 4: "score16_sym_simt_kernel", 5: "kde1d_kernel", 6: "kde1d_score_kernel",
-                7: "score16_tc_kernel", 8: "score16_sym_tc_kernel"}
+                7: "score16_tc_kernel"}
 
 
 def parse():
@@ -58,6 +58,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["fsk", "reference"], default="fsk")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--op", choices=["kde16", "score16"], default=None,
+                    help="time one operation alone on n GMM8 points (profiling case; no contract line)")
+    ap.add_argument("--n", type=int, default=N_TRAIN, help="points for --op (queries = data)")
     return ap.parse_args()
 
 
@@ -380,8 +383,45 @@ def run_gpu_arm(args) -> None:
         dist.destroy_process_group()
 
 
+def run_op(args) -> None:
+    """One operation alone (the profiling case for ncu captures): n GMM8
+    points as data and as queries, Silverman bandwidth, W warm-up and K timed
+    launches with CUDA events on the launching stream."""
+    import torch
+
+    import __graft_entry__ as ge
+
+    ge.build()
+    from fsk import ops, workloads
+
+    dev = torch.device("cuda", 0)
+    x = torch.from_numpy(workloads.GMM16(seed=0).sample(args.n, seed=1)).to(dev)
+    h = float(ops.silverman(x).item())
+    if args.op == "kde16":
+        fn = lambda: ops.kde16_sum(x, x, h)
+    else:
+        fn = lambda: ops.empscore16(x, h)
+    for _ in range(args.warmup):
+        fn()
+    torch.cuda.synchronize(dev)
+    s_ev, e_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stream = torch.cuda.current_stream(dev)
+    s_ev.record(stream)
+    for _ in range(args.steps):
+        fn()
+    e_ev.record(stream)
+    torch.cuda.synchronize(dev)
+    ops.device_status(dev)
+    ms = s_ev.elapsed_time(e_ev) / args.steps
+    print(json.dumps({"op": args.op, "n": args.n, "h": h, "ms_per_call": ms,
+                      "pair_evals_per_s": float(args.n) * args.n / (ms * 1e-3)}), flush=True)
+
+
 def main():
     args = parse()
+    if args.op:
+        run_op(args)
+        return
     if args.impl == "reference":
         run_reference_arm(args)
     else:

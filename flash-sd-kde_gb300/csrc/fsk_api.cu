@@ -157,23 +157,32 @@ int fsk_kde16(const float* queries, int64_t m, const float* data, int64_t n, dou
 }
 
 // ---- empirical score ------------------------------------------------------------
-static size_t empscore_bytes(int64_t n, int variant, int splits) {
+// Tensor precision: the tcgen05 ordered kernel for both variants (the
+// symmetric variant is the same quantity; on GB300 the tensor-core product
+// is cheaper than halving the exps on CUDA cores).  FSK_PREC_IEEE: the
+// CUDA-core kernels of the requested variant.
+static size_t empscore_bytes(int64_t n, int variant, int flags) {
   WsCarver c(nullptr, 0);
   take_center(c, n);
-  if (variant == FSK_SCORE_SYMMETRIC) {
+  size_t b = c.used;
+  if (!(flags & FSK_PREC_IEEE)) {
+    b = align_up(b, 256) + tc::tc_score16_ws_bytes(tc::plan_score16(n), n);
+  } else if (variant == FSK_SCORE_SYMMETRIC) {
     c.take<double>((size_t)n);
     c.take<double>((size_t)n * FSK_D);
+    b = c.used;
   } else {
+    const int splits = simt_score16_splits(n);
     c.take<double>((size_t)splits * n);
     c.take<double>((size_t)splits * n * FSK_D);
+    b = c.used;
   }
-  return align_up(c.used, 256);
+  return align_up(b, 256);
 }
 
 size_t fsk_empscore16_workspace_bytes(int64_t n, int variant, int flags) {
-  (void)flags;
   if (n < 1) return 0;
-  return empscore_bytes(n, variant, simt_score16_splits(n));
+  return empscore_bytes(n, variant, flags);
 }
 
 int fsk_empscore16(const float* data, int64_t n, double bandwidth, int variant, int flags, float* pdf_sum,
@@ -184,25 +193,33 @@ int fsk_empscore16(const float* data, int64_t n, double bandwidth, int variant, 
   int st = check_device();
   if (st) return st;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const int splits = simt_score16_splits(n);
-  if (!workspace || workspace_bytes < empscore_bytes(n, variant, splits)) return FSK_ERR_WORKSPACE_TOO_SMALL;
+  if (!workspace || workspace_bytes < empscore_bytes(n, variant, flags)) return FSK_ERR_WORKSPACE_TOO_SMALL;
   WsCarver c(workspace, workspace_bytes);
   CenterBufs cb = take_center(c, n);
   launch_mean16(data, n, cb.scratch, cb.mu, cb.mu64, s);
   const bool fm = (flags & FSK_WEIGHTED_FEATURE_MAJOR) != 0;
   const int64_t ws_row = fm ? 1 : FSK_D, ws_col = fm ? n : 1;
-  if (variant == FSK_SCORE_SYMMETRIC) {
+  if (!(flags & FSK_PREC_IEEE)) {
+    const tc::TcPlan pl = tc::plan_score16(n);
+    double *ppdf = nullptr, *pw = nullptr;
+    st = tc::launch_score16_tc(data, n, cb.mu, bandwidth, pl, c, &ppdf, &pw, s);
+    if (st) return st;
+    launch_reduce_score(ppdf, pw, (int)(2 * pl.splits), (int)pl.splits, n, cb.mu64, data, pdf_sum,
+                        weighted_sum, ws_row, ws_col, s);
+  } else if (variant == FSK_SCORE_SYMMETRIC) {
     double* apdf = c.take<double>((size_t)n);
     double* aw = c.take<double>((size_t)n * FSK_D);
     launch_zero(apdf, n, s);
     launch_zero(aw, n * FSK_D, s);
     launch_score16_sym_simt(data, n, cb.mu, bandwidth, apdf, aw, s);
-    launch_reduce_score(apdf, aw, 1, n, cb.mu64, pdf_sum, weighted_sum, ws_row, ws_col, s);
+    launch_reduce_score(apdf, aw, 1, 1, n, cb.mu64, nullptr, pdf_sum, weighted_sum, ws_row, ws_col, s);
   } else {
+    const int splits = simt_score16_splits(n);
     double* ppdf = c.take<double>((size_t)splits * n);
     double* pw = c.take<double>((size_t)splits * n * FSK_D);
     launch_score16_simt(data, n, cb.mu, bandwidth, splits, ppdf, pw, s);
-    launch_reduce_score(ppdf, pw, splits, n, cb.mu64, pdf_sum, weighted_sum, ws_row, ws_col, s);
+    launch_reduce_score(ppdf, pw, splits, splits, n, cb.mu64, nullptr, pdf_sum, weighted_sum, ws_row, ws_col,
+                        s);
   }
   return cuda_status(cudaGetLastError());
 }
@@ -301,6 +318,13 @@ int fsk_diag_mma_probe(const float* a, const float* b, float* d, void* stream) {
   int st = check_device();
   if (st) return st;
   return tc::launch_mma_probe(a, b, d, static_cast<cudaStream_t>(stream));
+}
+
+int fsk_diag_mma_ts_probe(const float* a, const float* b, float* d, void* stream) {
+  if (!a || !b || !d) return FSK_ERR_INVALID_ARGUMENT;
+  int st = check_device();
+  if (st) return st;
+  return tc::launch_mma_ts_probe(a, b, d, static_cast<cudaStream_t>(stream));
 }
 
 }  // extern "C"

@@ -78,28 +78,34 @@ void launch_reduce_rows(const double* partials, int splits, int64_t m, double sc
   count_launch();
 }
 
+// pdf = sum of pdf partials, weighted = sum of centred partials + mu * pdf.
+// self_x != nullptr: the partials leave the self pair out; it is added here
+// exactly (phi_ii = 1, weight x_i).
 __global__ void reduce_score_kernel(const double* __restrict__ ppdf, const double* __restrict__ pw,
-                                    int splits, int64_t n, const double* __restrict__ mu64,
-                                    float* __restrict__ pdf, float* __restrict__ w, int64_t ws_row,
-                                    int64_t ws_col) {
+                                    int pdf_splits, int w_splits, int64_t n, const double* __restrict__ mu64,
+                                    const float* __restrict__ self_x, float* __restrict__ pdf,
+                                    float* __restrict__ w, int64_t ws_row, int64_t ws_col) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double p = 0.0;
-  for (int s = 0; s < splits; ++s) p += ppdf[(int64_t)s * n + i];
+  for (int s = 0; s < pdf_splits; ++s) p += ppdf[(int64_t)s * n + i];
+  const double p_other = p;
+  if (self_x) p += 1.0;
   pdf[i] = (float)p;
   for (int k = 0; k < FSK_D; ++k) {
     double a = 0.0;
-    for (int s = 0; s < splits; ++s) a += pw[((int64_t)s * n + i) * FSK_D + k];
-    w[i * ws_row + k * ws_col] = (float)(a + mu64[k] * p);
+    for (int s = 0; s < w_splits; ++s) a += pw[((int64_t)s * n + i) * FSK_D + k];
+    const double v = self_x ? a + mu64[k] * p_other + (double)self_x[i * FSK_D + k] : a + mu64[k] * p;
+    w[i * ws_row + k * ws_col] = (float)v;
   }
 }
 
-void launch_reduce_score(const double* ppdf, const double* pw, int splits, int64_t n,
-                         const double* mu64, float* pdf, float* w, int64_t ws_row, int64_t ws_col,
-                         cudaStream_t s) {
+void launch_reduce_score(const double* ppdf, const double* pw, int pdf_splits, int w_splits, int64_t n,
+                         const double* mu64, const float* self_x, float* pdf, float* w, int64_t ws_row,
+                         int64_t ws_col, cudaStream_t s) {
   const int T = 128;
-  reduce_score_kernel<<<(unsigned)((n + T - 1) / T), T, 0, s>>>(ppdf, pw, splits, n, mu64, pdf, w,
-                                                               ws_row, ws_col);
+  reduce_score_kernel<<<(unsigned)((n + T - 1) / T), T, 0, s>>>(ppdf, pw, pdf_splits, w_splits, n, mu64,
+                                                               self_x, pdf, w, ws_row, ws_col);
   count_launch();
 }
 

@@ -45,7 +45,7 @@ struct TcScales {
   float a_scale;   // alpha part scale  2^-ea  (A bias col holds alpha*a_scale, B holds 1/a_scale)
   float b_scale;   // beta part scale   2^-eb
   float out_mul;   // a2 = out_mul * D  (1 unless the product had to be scaled down)
-  int pad[3];
+  int pad[3];      // ea, eb, ew: x'' = (x - mu) 2^ew is the weighted-sum operand
 };
 
 struct TcParams {
@@ -68,12 +68,30 @@ struct TcPlan {
   int grid;
 };
 
+// Fills splits / tiles_per_split / grid from q_blocks and n_tiles.
+void plan_splits(TcPlan& pl);
 TcPlan plan_kde16(int64_t m, int64_t n);
+
+// Prep kernels shared by the tensor-core kernels (fsk_tc_kde16.cu).
+__global__ void scale_init_kernel(TcScales* sc);
+__global__ void scale_stats_kernel(const float* __restrict__ pts, int64_t count, const float* __restrict__ mu,
+                                   float c2, int is_query, float alpha_off, TcScales* __restrict__ sc);
+__global__ void scale_select_kernel(TcScales* sc);
+__global__ void prep_query_kernel(const float* __restrict__ q, int64_t m, int64_t m_pad,
+                                  const float* __restrict__ mu, float c2, float alpha_off,
+                                  const TcScales* __restrict__ sc, uint8_t* __restrict__ img,
+                                  float* __restrict__ qexact);
 size_t tc_kde16_ws_bytes(const TcPlan& pl, int64_t m, bool atomic);
 int launch_kde16_tc(const float* q, int64_t m, const float* x, int64_t n, const float* mu, double h,
                     bool laplace, const TcPlan& pl, WsCarver& c, double** partials_out, bool atomic,
                     cudaStream_t s);
+TcPlan plan_score16(int64_t n);
+size_t tc_score16_ws_bytes(const TcPlan& pl, int64_t n);
+// Empirical-score partials: ppdf [2 * splits][n], pw [splits][n][16] (centred).
+int launch_score16_tc(const float* x, int64_t n, const float* mu, double h, const TcPlan& pl, WsCarver& c,
+                      double** ppdf_out, double** pw_out, cudaStream_t s);
 int launch_mma_probe(const float* a, const float* b, float* d, cudaStream_t s);
+int launch_mma_ts_probe(const float* a, const float* b, float* d, cudaStream_t s);
 int launch_wait_timeout_probe(int* out, cudaStream_t s);
 
 // fp16 core-matrix offset of element (row r, k) in an image whose rows are

@@ -58,7 +58,9 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
   uint64_t* tempty = bars + 2 * NS + 2;  // [2] accumulator buffer drained
   uint64_t* qready = bars + 2 * NS + 4;  // query images loaded
   uint64_t* qempty = bars + 2 * NS + 5;  // query images no longer read by the MMA
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * NS + 6);
+  uint64_t* drain = bars + 2 * NS + 6;   // all MMAs of this CTA finished (exit path)
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * NS + 7);
+  int64_t n_stage_copies = 0, n_query_copies = 0;   // producer: bulk copies issued
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -74,6 +76,7 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
     }
     mbar_init(qready, 1);
     mbar_init(qempty, 1);
+    mbar_init(drain, 1);
     fence_barrier_init();
   }
   if (warp == MMA_WARP) {
@@ -93,19 +96,22 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
 
   if (warp == PRODUCER_WARP) {
     if (lane == 0) {
-      int64_t g = 0, k = 0;
-      for (int64_t u = u_begin; u < u_end; ++u, ++k) {
+      int64_t& g = n_stage_copies;
+      int64_t& k = n_query_copies;
+      for (int64_t u = u_begin; u < u_end; ++u) {
         const int64_t qb = u / p.splits, sp = u % p.splits;
         if (!mbar_wait(qempty, (uint32_t)((k & 1) ^ 1), 1)) goto done;
         mbar_arrive_expect_tx(qready, A_BYTES);
         bulk_g2s(sA, p.qimg + qb * (int64_t)A_BYTES, A_BYTES, qready);
+        ++k;
         const int64_t t0 = sp * p.tiles_per_split;
         const int64_t t1 = imin<int64_t>(p.n_tiles, t0 + p.tiles_per_split);
-        for (int64_t t = t0; t < t1; ++t, ++g) {
+        for (int64_t t = t0; t < t1; ++t) {
           const int s = (int)(g % NS);
           if (!mbar_wait(&empty[s], (uint32_t)(((g / NS) & 1) ^ 1), 2)) goto done;
           mbar_arrive_expect_tx(&full[s], B_STAGE_BYTES);
           bulk_g2s(sB + s * B_STAGE_BYTES, p.ximg + t * (int64_t)B_STAGE_BYTES, B_STAGE_BYTES, &full[s]);
+          ++g;
         }
       }
     }
@@ -282,6 +288,17 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
     }
   }
 done:
+  // Exit path (also after a timed-out wait): let this CTA's bulk copies and
+  // MMAs finish before shared and tensor memory are released.
+  if (warp == PRODUCER_WARP && lane == 0) {
+    for (int64_t i = imax<int64_t>(0, n_stage_copies - NS); i < n_stage_copies; ++i)
+      mbar_wait(&full[i % NS], (uint32_t)((i / NS) & 1), 7);
+    if (n_query_copies > 0) mbar_wait(qready, (uint32_t)((n_query_copies - 1) & 1), 8);
+  }
+  if (warp == MMA_WARP && lane == 0) {
+    mma_commit(drain);
+    mbar_wait(drain, 0, 9);
+  }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -292,7 +309,7 @@ done:
 // Maxima for the scale selection: |2 c2 (q-mu)|, c2 |q-mu|^2 over queries and
 // |x-mu|, c2 |x-mu|^2 over data.  One thread per row; block-reduced.
 __global__ void scale_stats_kernel(const float* __restrict__ pts, int64_t count, const float* __restrict__ mu,
-                                   float c2, int is_query, TcScales* __restrict__ sc) {
+                                   float c2, int is_query, float alpha_off, TcScales* __restrict__ sc) {
   float vmax = 0.f, nmax = 0.f;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -304,7 +321,7 @@ __global__ void scale_stats_kernel(const float* __restrict__ pts, int64_t count,
       mx = fmaxf(mx, fabsf(v));
     }
     vmax = fmaxf(vmax, is_query ? 2.0f * c2 * mx : mx);
-    nmax = fmaxf(nmax, c2 * nrm);
+    nmax = fmaxf(nmax, fabsf(c2 * nrm - (is_query ? alpha_off : 0.f)));
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
@@ -352,6 +369,8 @@ __global__ void scale_select_kernel(TcScales* sc) {
   sc->b_scale = ldexpf(1.f, -es - eb);    // beta * b_scale in B, 2^eb in A
   sc->pad[0] = ea;
   sc->pad[1] = eb;
+  // scale of the (x - mu) operand of the weighted-sum product: max |x'| <= T
+  sc->pad[2] = (int)floor(log2((double)T / (double)lx));
   sc->out_mul = ldexpf(1.f, es);
 }
 
@@ -383,8 +402,9 @@ __global__ void prep_data_kernel(const float* __restrict__ x, int64_t n, int64_t
 // query tile image: [H (QT x 32 fp16) | L (QT x 16 fp16)], plus the original
 // coordinates for the exact recompute.
 __global__ void prep_query_kernel(const float* __restrict__ q, int64_t m, int64_t m_pad,
-                                  const float* __restrict__ mu, float c2, const TcScales* __restrict__ sc,
-                                  uint8_t* __restrict__ img, float* __restrict__ qexact) {
+                                  const float* __restrict__ mu, float c2, float alpha_off,
+                                  const TcScales* __restrict__ sc, uint8_t* __restrict__ img,
+                                  float* __restrict__ qexact) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m_pad) return;
   const bool ok = i < m;
@@ -399,18 +419,13 @@ __global__ void prep_query_kernel(const float* __restrict__ q, int64_t m, int64_
     v[k] = ok ? cv * qs : 0.f;
   }
   uint8_t* tile = img + (i / QT) * (int64_t)A_TILE_BYTES;
-  const float alpha = ok ? -c2 * nrm * sc->a_scale : 0.f;
+  const float alpha = ok ? (alpha_off - c2 * nrm) * sc->a_scale : 0.f;
   write_operand_row(tile, tile + A_H_BYTES, (int)(i % QT), v, alpha, ok ? ldexpf(1.f, sc->pad[1]) : 0.f, false);
 #pragma unroll
   for (int k = 0; k < FSK_D; ++k) qexact[i * FSK_D + k] = qo[k];
 }
 
-TcPlan plan_kde16(int64_t m, int64_t n) {
-  TcPlan pl;
-  pl.m_pad = (m + NQT * QT - 1) / (NQT * QT) * (NQT * QT);
-  pl.n_tiles = (n + NT - 1) / NT;
-  pl.n_pad = pl.n_tiles * NT;
-  pl.q_blocks = pl.m_pad / (NQT * QT);
+void plan_splits(TcPlan& pl) {
   const int64_t sms = sm_count();
   // Data splits only add parallelism: pick the smallest split count giving
   // every CTA >= 4 units with a near-integral number of units per CTA.
@@ -433,6 +448,15 @@ TcPlan plan_kde16(int64_t m, int64_t n) {
   pl.tiles_per_split = (pl.n_tiles + best - 1) / best;
   pl.splits = (pl.n_tiles + pl.tiles_per_split - 1) / pl.tiles_per_split;  // all splits non-empty
   pl.grid = (int)imin<int64_t>(pl.q_blocks * pl.splits, sms);
+}
+
+TcPlan plan_kde16(int64_t m, int64_t n) {
+  TcPlan pl;
+  pl.m_pad = (m + NQT * QT - 1) / (NQT * QT) * (NQT * QT);
+  pl.n_tiles = (n + NT - 1) / NT;
+  pl.n_pad = pl.n_tiles * NT;
+  pl.q_blocks = pl.m_pad / (NQT * QT);
+  plan_splits(pl);
   return pl;
 }
 
@@ -464,15 +488,16 @@ int launch_kde16_tc(const float* q, int64_t m, const float* x, int64_t n, const 
   count_launch();
   const int sblocks_q = (int)imin<int64_t>(1024, (m + 255) / 256);
   const int sblocks_x = (int)imin<int64_t>(1024, (n + 255) / 256);
-  scale_stats_kernel<<<sblocks_q, 256, 0, s>>>(q, m, mu, c2, 1, sc);
+  scale_stats_kernel<<<sblocks_q, 256, 0, s>>>(q, m, mu, c2, 1, 0.f, sc);
   count_launch();
-  scale_stats_kernel<<<sblocks_x, 256, 0, s>>>(x, n, mu, c2, 0, sc);
+  scale_stats_kernel<<<sblocks_x, 256, 0, s>>>(x, n, mu, c2, 0, 0.f, sc);
   count_launch();
   scale_select_kernel<<<1, 32, 0, s>>>(sc);
   count_launch();
   prep_data_kernel<<<(unsigned)((pl.n_pad + 255) / 256), 256, 0, s>>>(x, n, pl.n_pad, mu, c2, sc, ximg);
   count_launch();
-  prep_query_kernel<<<(unsigned)((pl.m_pad + 255) / 256), 256, 0, s>>>(q, m, pl.m_pad, mu, c2, sc, qimg, qexact);
+  prep_query_kernel<<<(unsigned)((pl.m_pad + 255) / 256), 256, 0, s>>>(q, m, pl.m_pad, mu, c2, 0.f, sc, qimg,
+                                                                        qexact);
   count_launch();
   if (atomic) launch_zero(part, m, s);
 

@@ -179,11 +179,12 @@ def emp_sd_kde_fit_transform(
     train = ops.as_matrix(data, device, ND_FEATURES)
     if train.shape[0] == 0:
         raise ValueError("data must be non-empty.")
+    prec = "ieee" if precision_mode == PRECISION_FP32_IEEE else "tensor"
     if emp_score_backend == EMP_SCORE_BACKEND_SYMMETRIC_ATOMIC:
-        pdf_sum, weighted_sum = ops.empscore16(train, bandwidth, variant="symmetric")
+        pdf_sum, weighted_sum = ops.empscore16(train, bandwidth, variant="symmetric", precision=prec)
     else:
         pdf_sum, weighted_sum = ops.empscore16(
-            train, bandwidth, variant="ordered",
+            train, bandwidth, variant="ordered", precision=prec,
             feature_major=emp_score_backend == EMP_SCORE_BACKEND_FLASH_SD_KDE)
     if return_debug:
         debiased, score = ops.debias16(train, pdf_sum, weighted_sum, bandwidth, eps, return_score=True)

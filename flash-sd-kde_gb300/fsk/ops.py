@@ -111,8 +111,12 @@ def empscore16(
     *,
     variant: str = "ordered",
     feature_major: bool = False,
+    precision: str = "tensor",
 ) -> tuple[torch.Tensor, torch.Tensor]:
-    """(pdf_sum (n,), weighted_sum (n,16)); feature_major returns a (16,n)-backed view."""
+    """(pdf_sum (n,), weighted_sum (n,16)); feature_major returns a (16,n)-backed view.
+
+    precision "tensor": the tcgen05 kernel (both variants); "ieee": the
+    CUDA-core kernel of the requested variant."""
     h = _check_bw(bandwidth)
     dev = _device(data.device)
     x = as_matrix(data, dev)
@@ -121,6 +125,7 @@ def empscore16(
         raise ValueError("data must contain at least one element.")
     var = L.FSK_SCORE_SYMMETRIC if variant == "symmetric" else L.FSK_SCORE_ORDERED
     flags = L.FSK_WEIGHTED_FEATURE_MAJOR if feature_major else 0
+    flags |= L.FSK_PREC_IEEE if precision == "ieee" else L.FSK_PREC_TENSOR
     lib = L.load()
     with torch.cuda.device(dev):
         pdf = torch.empty(n, dtype=torch.float32, device=dev)
@@ -252,4 +257,18 @@ def mma_probe(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
         d = torch.empty((128, 64), dtype=torch.float32, device=dev)
         st = L.load().fsk_diag_mma_probe(a.data_ptr(), b.data_ptr(), d.data_ptr(), _stream(dev))
     L.check(st, "fsk_diag_mma_probe")
+    return d
+
+
+def mma_ts_probe(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
+    """tcgen05.mma with fp16(a) (128,64) read from tensor memory, by fp16(b) (16,64)^T -> (128,16)."""
+    dev = _device(a.device)
+    a = a.to(device=dev, dtype=torch.float32).contiguous()
+    b = b.to(device=dev, dtype=torch.float32).contiguous()
+    if a.shape != (128, 64) or b.shape != (16, 64):
+        raise ValueError("probe operands must be (128, 64) and (16, 64)")
+    with torch.cuda.device(dev):
+        d = torch.empty((128, 16), dtype=torch.float32, device=dev)
+        st = L.load().fsk_diag_mma_ts_probe(a.data_ptr(), b.data_ptr(), d.data_ptr(), _stream(dev))
+    L.check(st, "fsk_diag_mma_ts_probe")
     return d

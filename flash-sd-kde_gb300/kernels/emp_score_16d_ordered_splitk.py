@@ -30,4 +30,5 @@ def emp_score_16d_ordered_splitk(
         raise ValueError("data must be non-empty.")
     if precision_mode not in {PRECISION_FAST_TF32, PRECISION_FP32_IEEE}:
         raise ValueError(f"invalid precision_mode {precision_mode}.")
-    return ops.empscore16(train, bandwidth, variant="ordered")
+    prec = "ieee" if precision_mode == PRECISION_FP32_IEEE else "tensor"
+    return ops.empscore16(train, bandwidth, variant="ordered", precision=prec)

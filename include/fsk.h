@@ -173,6 +173,12 @@ FSK_API int64_t fsk_launch_count(void);
  * kernel uses; inputs are FP32 rounded to fp16, d is (128,64) FP32
  * row-major.  The tests compare it with a host dot product. */
 FSK_API int fsk_diag_mma_probe(const float* a, const float* b, float* d, void* stream);
+/* Tensor-memory operand probe, no counterpart in the reference: four K=16
+ * tcgen05.mma steps (fp16, FP32 accumulate, M=128, N=16) with the A operand
+ * a (128,64) stored to tensor memory (two fp16 per column) and b (16,64) in
+ * the score kernel's transposed-feature image layout; d is (128,16) FP32
+ * row-major, a . b^T of the fp16-rounded inputs. */
+FSK_API int fsk_diag_mma_ts_probe(const float* a, const float* b, float* d, void* stream);
 /* Failure-path probe, no counterpart in the reference: a kernel waits on an
  * mbarrier nothing arrives on; its bounded wait gives up after about 2 s,
  * writes 0 to *out (device int) and records FSK_ERR_DEVICE_TIMEOUT, which the
@@ -187,7 +193,7 @@ FSK_API int fsk_diag_pipe_rates(double* rates_out, void* stream);
 /* ---- measurement hooks (no counterpart in the reference) ------------------ */
 /* Kernel ids: 1 tensor-core 16-D KDE, 2 CUDA-core 16-D KDE, 3 CUDA-core
  * ordered score, 4 CUDA-core symmetric score, 5 1-D KDE, 6 1-D KDE score,
- * 7 tensor-core ordered score, 8 tensor-core symmetric score. */
+ * 7 tensor-core score. */
 /* When enabled, each hot-path kernel launch is bracketed by CUDA events on
  * its own stream. */
 FSK_API void fsk_timer_enable(int on);

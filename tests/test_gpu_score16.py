@@ -21,6 +21,24 @@ def _close(a, b, rtol=1e-5, floor=1e-5):
     np.testing.assert_allclose(a, b, rtol=rtol, atol=floor * np.abs(b).max())
 
 
+def test_mma_ts_probe_layout(cuda_dev):
+    """Four K=16 tcgen05.mma steps (fp16, M=128, N=16) with the A operand in
+    tensor memory (two fp16 per column) and B in the transposed-feature image
+    layout equal the host product of the fp16-rounded operands: pins the
+    A-in-TMEM packing, the 128-byte-row descriptors and the N=16 instruction
+    descriptor used by the score kernel's weighted-sum product."""
+    from fsk import ops
+
+    g = torch.Generator().manual_seed(1)
+    a = torch.rand(128, 64, generator=g) * 4
+    b = torch.randn(16, 64, generator=g) * 3
+    d = ops.mma_ts_probe(a.to(cuda_dev), b.to(cuda_dev)).cpu().double()
+    ah, bh = a.half().double(), b.half().double()
+    ref = ah @ bh.T
+    scale = ah.abs() @ bh.abs().T
+    assert ((d - ref).abs() <= 2e-6 * scale + 1e-30).all(), float(((d - ref).abs() / scale).max())
+
+
 @pytest.mark.parametrize("seed", [2, 3, 4, 10])
 @pytest.mark.parametrize("variant", ["ordered", "symmetric"])
 def test_score_vs_reference(cuda_dev, golden, seed, variant):
