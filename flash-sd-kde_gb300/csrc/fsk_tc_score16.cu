@@ -18,21 +18,26 @@
 //    recompute of the KDE kernel (the recomputed value also replaces the
 //    approximate one in the weights), then the weights are split into fp16
 //    hi + lo and stored to tensor memory with tcgen05.st.
-//  * W += Phi_hi X_hi + Phi_hi X_lo + Phi_lo X_hi: tcgen05.mma with the A
-//    operand (weights, M=128 x K=64) read from tensor memory and the B operand
-//    ((x_j - mu) 2^ew, fp16 hi/lo, K-major over the data points) from the
-//    data stage in shared memory, N = 16 features, FP32 accumulation over a
-//    group of S_GROUP tiles, then added into compensated FP32 sums.
+//  * The weights are written back into the tensor-memory columns their S
+//    came from, as fp16 hi | lo, and
+//    W += (Phi_hi + Phi_lo) [X_hi | X_lo]: tcgen05.mma with the A operand
+//    (weights, M=128 x K=64) read from tensor memory and the B operand
+//    ((x_j - mu) 2^ew as fp16 hi and lo rows, K-major over the data points)
+//    from the data stage, N = 32, FP32 accumulation over a group of S_GROUP
+//    tiles, then added into compensated FP32 sums.
 //
 // Pipeline (one persistent CTA per SM, 18 warps):
 //   warp 16 : producer (bulk copies of query images per unit, data stages).
-//   warp 17 : owns TMEM, issues S(t) then W(t-1) (one lane).
+//   warp 17 : owns TMEM; issues S up to NBUF tiles ahead of W (one lane).
+//             An M=128, K=16 tcgen05.mma costs ~46 cycles whatever N <= 64
+//             is, so the weighted-sum product is the expensive part: two
+//             N=32 MMAs per K step, and the epilogue never waits for it.
 //   warps 0-15: epilogue; warp w: query tile w/8, data-column half (w/4)&1,
 //             TMEM lane quarter w&3.  The two column halves of a row keep
 //             separate pdf partials (written as two virtual splits) and
 //             read disjoint halves of the weighted-sum features.
-// TMEM: S [2 buffers][2 query tiles][64] | Phi [2 tiles][hi 32 | lo 32]
-//       | W [2 group parities][2 tiles][16].
+// TMEM: S / weights [NBUF buffers][2 query tiles][64]
+//       | W [2 group parities][2 tiles][X_hi part 16 | X_lo part 16].
 #include <cuda_fp16.h>
 
 #include "fsk_kernels.cuh"
@@ -45,7 +50,7 @@ namespace tc {
 namespace {
 
 constexpr int SNQT = 2;                                    // query tiles per unit (256 queries)
-constexpr int SNS = 8;                                     // data stages
+constexpr int SNS = 6;                                     // data stages
 constexpr int XT_ROW_BYTES = NT * 2;                       // one feature row over 64 points, fp16
 constexpr int XT_BYTES = FSK_D * XT_ROW_BYTES;             // 2 KB
 constexpr int S_XTH_OFFSET = B_H_BYTES + B_L_BYTES;        // 6 KB
@@ -57,19 +62,32 @@ constexpr int S_EPI_WARPS = 8 * SNQT;
 constexpr int S_PRODUCER_WARP = S_EPI_WARPS;
 constexpr int S_MMA_WARP = S_EPI_WARPS + 1;
 constexpr int S_THREADS = (S_EPI_WARPS + 2) * 32;
-constexpr int S_GROUP = 4;                                 // data tiles per W accumulation
+constexpr int S_GROUP = 8;                                 // data tiles per W accumulation
+constexpr int NBUF = 3;                                    // S / weight buffers in TMEM
+constexpr int WN = 2 * FSK_D;                              // W MMA N: X_hi and X_lo rows
 constexpr int T_S = 0;
-constexpr int T_PHI = 2 * SNQT * NT;                       // 256
-constexpr int T_W = T_PHI + SNQT * NT;                     // 384
+constexpr int T_W = NBUF * SNQT * NT;                      // 384
 constexpr int S_TMEM_COLS = 512;
 // exact-recompute corrections of the weighted sums: [unit parity][column half][256 rows][16] FP32
-constexpr int S_WCORR_OFFSET = S_A_BYTES + SNS * S_STAGE_BYTES + 512;
+// original coordinates of the unit's 256 queries (exact near-pair recompute)
+constexpr int S_QX_OFFSET = S_A_BYTES;
+constexpr int S_QX_BYTES = SNQT * QT * FSK_D * 4;                    // 16 KB
+constexpr int S_B_OFFSET = S_QX_OFFSET + S_QX_BYTES;
+constexpr int S_BAR_OFFSET = S_B_OFFSET + SNS * S_STAGE_BYTES;
+constexpr int S_WCORR_OFFSET = S_BAR_OFFSET + 512;
 constexpr int S_WCORR_BYTES = 2 * 2 * SNQT * QT * FSK_D * 4;          // 64 KB
-constexpr int S_SMEM_BYTES = S_WCORR_OFFSET + S_WCORR_BYTES;
+// compensated per-thread weighted-sum accumulators (8 features, value + error),
+// float4 planes [s0-3, s4-7, c0-3, c4-7][epilogue thread]
+constexpr int S_WACC_OFFSET = S_WCORR_OFFSET + S_WCORR_BYTES;
+constexpr int S_WACC_BYTES = 4 * S_EPI_WARPS * 32 * 16;                // 32 KB
+constexpr int S_MU_OFFSET = S_WACC_OFFSET + S_WACC_BYTES;             // data mean, 16 FP32
+constexpr int S_SMEM_BYTES = S_MU_OFFSET + FSK_D * 4;
 constexpr float PHI_LOG2_SCALE = 15.0f;                    // weights are phi * 2^15
-static_assert(T_W + 2 * SNQT * FSK_D <= S_TMEM_COLS, "TMEM budget");
-static_assert(S_STAGE_BYTES % 16 == 0 && S_A_BYTES % 16 == 0, "bulk copy granularity");
+static_assert(T_W + 2 * SNQT * WN <= S_TMEM_COLS, "TMEM budget");
+static_assert(S_XTL_OFFSET == S_XTH_OFFSET + 16 * XT_ROW_BYTES, "X_lo rows follow X_hi rows (one N=32 operand)");
+static_assert(S_STAGE_BYTES % 16 == 0 && S_A_BYTES % 16 == 0 && S_QX_BYTES % 16 == 0, "bulk copy granularity");
 static_assert(S_SMEM_BYTES <= 227 * 1024, "shared memory");
+static_assert((2 * SNS + 6 + NBUF * SNQT + 8) * 8 + 4 <= 512, "barrier area");
 
 struct ScParams {
   const uint8_t* qimg;
@@ -94,25 +112,54 @@ __device__ __forceinline__ void split_pack(float v0, float v1, uint32_t& hi, uin
   lo = *reinterpret_cast<const uint32_t*>(&l);
 }
 
+// Walks the (unit, data tile) sequence of one CTA: units are (query block,
+// data split), each split covers tiles [t0, t1).
+struct TileCursor {
+  int u, u_end, splits, tps, n_tiles, t0, t1, t;
+  __device__ void start(int ub, int ue, int sp_count, int tiles_per_split, int tiles) {
+    u = ub; u_end = ue; splits = sp_count; tps = tiles_per_split; n_tiles = tiles;
+    enter();
+  }
+  __device__ void enter() {
+    if (u < u_end) {
+      t0 = (u % splits) * tps;
+      t1 = min(n_tiles, t0 + tps);
+      t = t0;
+    }
+  }
+  __device__ bool done() const { return u >= u_end; }
+  __device__ void next() {
+    if (++t >= t1) {
+      ++u;
+      enter();
+    }
+  }
+};
+
 __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* sA = smem_raw;
-  uint8_t* sB = smem_raw + S_A_BYTES;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + S_A_BYTES + SNS * S_STAGE_BYTES);
+  const float* sQ = reinterpret_cast<const float*>(smem_raw + S_QX_OFFSET);
+  uint8_t* sB = smem_raw + S_B_OFFSET;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + S_BAR_OFFSET);
+  float* sMu = reinterpret_cast<float*>(smem_raw + S_MU_OFFSET);
   uint64_t* full = bars;                      // [SNS] stage loaded
   uint64_t* empty = bars + SNS;               // [SNS] stage consumed (W MMA + epilogue)
-  uint64_t* tfull = bars + 2 * SNS;           // [2] S buffer written
-  uint64_t* tempty = bars + 2 * SNS + 2;      // [2] S buffer read
-  uint64_t* pready = bars + 2 * SNS + 4;      // [SNQT] weights of a tile stored
-  uint64_t* pfree = bars + 2 * SNS + 6;       // [SNQT] weights consumed by the W MMA
-  uint64_t* wfull = bars + 2 * SNS + 8;       // [2] W group accumulated
-  uint64_t* wempty = bars + 2 * SNS + 10;     // [2] W group read
-  uint64_t* qready = bars + 2 * SNS + 12;
-  uint64_t* qempty = bars + 2 * SNS + 13;
-  uint64_t* drain = bars + 2 * SNS + 14;      // all MMAs of this CTA finished (exit path)
-  uint64_t* cready = bars + 2 * SNS + 15;     // unit's W corrections written (epilogue warps)
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * SNS + 16);
+  uint64_t* tfull = bars + 2 * SNS;           // [NBUF] S buffer written
+  uint64_t* wdone = bars + 2 * SNS + 3;       // [NBUF] W MMA done reading the buffer's weights
+  // [NBUF][SNQT] weights of a query tile stored in a buffer.  One barrier per
+  // buffer: the epilogue may run NBUF tiles ahead of the W MMA, and a
+  // buffer's barrier cannot complete again before its weights are consumed.
+  uint64_t* pready = bars + 2 * SNS + 6;
+  uint64_t* wfull = bars + 2 * SNS + 6 + NBUF * SNQT;        // [2] W group accumulated
+  uint64_t* wempty = wfull + 2;                               // [2] W group read
+  uint64_t* qready = wfull + 4;
+  uint64_t* qempty = wfull + 5;
+  uint64_t* drain = wfull + 6;                // all MMAs of this CTA finished (exit path)
+  uint64_t* cready = wfull + 7;               // unit's W corrections written (epilogue warps)
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(wfull + 8);
   float* wcorr = reinterpret_cast<float*>(smem_raw + S_WCORR_OFFSET);
+  float4* wacc = reinterpret_cast<float4*>(smem_raw + S_WACC_OFFSET);
   int64_t n_stage_copies = 0, n_query_copies = 0;   // producer: bulk copies issued
 
   const int warp = threadIdx.x >> 5;
@@ -123,18 +170,17 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1 + S_EPI_WARPS);
     }
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < NBUF; ++b) {
       mbar_init(&tfull[b], 1);
-      mbar_init(&tempty[b], S_EPI_WARPS);
+      mbar_init(&wdone[b], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
       mbar_init(&wfull[b], 1);
       mbar_init(&wempty[b], S_EPI_WARPS);
     }
-    for (int a = 0; a < SNQT; ++a) {
-      mbar_init(&pready[a], 8);
-      mbar_init(&pfree[a], 1);
-    }
+    for (int i = 0; i < NBUF * SNQT; ++i) mbar_init(&pready[i], 8);
     mbar_init(qready, 1);
-    mbar_init(qempty, 1);
+    mbar_init(qempty, 1 + S_EPI_WARPS);   // last S MMA of the unit + every epilogue warp
     mbar_init(drain, 1);
     mbar_init(cready, S_EPI_WARPS);
     fence_barrier_init();
@@ -143,6 +189,7 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
     tmem_alloc(tmem_slot, S_TMEM_COLS);
     tmem_relinquish();
   }
+  if (threadIdx.x < FSK_D) sMu[threadIdx.x] = p.mu[threadIdx.x];
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -158,8 +205,9 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
       for (int64_t u = u_begin; u < u_end; ++u) {
         const int64_t qb = u / p.splits, sp = u % p.splits;
         if (!mbar_wait(qempty, (uint32_t)((k & 1) ^ 1), 21)) goto done;
-        mbar_arrive_expect_tx(qready, S_A_BYTES);
+        mbar_arrive_expect_tx(qready, S_A_BYTES + S_QX_BYTES);
         bulk_g2s(sA, p.qimg + qb * (int64_t)S_A_BYTES, S_A_BYTES, qready);
+        bulk_g2s(smem_raw + S_QX_OFFSET, p.qexact + qb * (int64_t)(SNQT * QT * FSK_D), S_QX_BYTES, qready);
         ++k;
         const int64_t t0 = sp * p.tiles_per_split;
         const int64_t t1 = imin<int64_t>(p.n_tiles, t0 + p.tiles_per_split);
@@ -175,20 +223,32 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
   } else if (warp == S_MMA_WARP) {
     if (lane == 0) {
       const uint32_t idesc_s = idesc_f16_f32(QT, NT);
-      const uint32_t idesc_w = idesc_f16_f32(QT, FSK_D);
-      int64_t g = 0, k = 0, grp = 0;
-      for (int64_t u = u_begin; u < u_end; ++u, ++k) {
-        const int64_t sp = u % p.splits;
-        if (!mbar_wait(qready, (uint32_t)(k & 1), 23)) goto done;
-        const int64_t t0 = sp * p.tiles_per_split;
-        const int64_t t1 = imin<int64_t>(p.n_tiles, t0 + p.tiles_per_split);
-        // iteration t issues S(t) (t < t1) and then W(t-1) (t > t0)
-        for (int64_t t = t0; t <= t1; ++t) {
-          if (t < t1) {
-            const int s = (int)(g % SNS);
-            const int b = (int)(g & 1);
-            if (!mbar_wait(&full[s], (uint32_t)((g / SNS) & 1), 24)) goto done;
-            if (!mbar_wait(&tempty[b], (uint32_t)(((g >> 1) & 1) ^ 1), 25)) goto done;
+      const uint32_t idesc_w = idesc_f16_f32(QT, WN);
+      // Two cursors over this CTA's tiles: S runs up to NBUF tiles ahead of W.
+      // Nothing here blocks: each pass issues S and/or W when all their
+      // barriers have completed (the next unit's query images, for instance,
+      // arrive only after the epilogue has read this unit's last W group, so
+      // waiting for them before issuing that W would deadlock).  One watchdog
+      // bounds the time without progress.
+      TileCursor cs, cw;
+      cs.start((int)u_begin, (int)u_end, (int)p.splits, (int)p.tiles_per_split, (int)p.n_tiles);
+      cw = cs;
+      int gs = 0, gw = 0, kq = 0, grp = 0;
+      bool q_held = false;   // query images of the S cursor's unit are resident
+      uint64_t idle_since = 0;
+      while (!cw.done()) {
+        bool progressed = false;
+        if (!cs.done() && gs < gw + NBUF) {
+          const int b = gs % NBUF;
+          const int s = gs % SNS;
+          if (cs.t == cs.t0 && !q_held && mbar_try_wait(qready, (uint32_t)(kq & 1))) {
+            q_held = true;
+            ++kq;
+          }
+          // the buffer's previous weights (tile gs - NBUF) must be consumed
+          if ((cs.t != cs.t0 || q_held) &&
+              (gs < NBUF || mbar_try_wait(&wdone[b], (uint32_t)(((gs - NBUF) / NBUF) & 1))) &&
+              mbar_try_wait(&full[s], (uint32_t)((gs / SNS) & 1))) {
             tc_fence_after();
             const uint32_t bs = smem_u32(sB + s * S_STAGE_BYTES);
             const uint64_t b_hf = smem_desc_kmajor(bs, 128, 8 * H_ROW_BYTES);
@@ -207,41 +267,65 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
               mma_f16_ss(d, a_hb, b_hb, idesc_s, 1u);
             }
             mma_commit(&tfull[b]);
-            if (t == t1 - 1) mma_commit(qempty);   // last read of the query images
+            if (cs.t == cs.t1 - 1) {
+              mma_commit(qempty);   // last S read of this unit's query images
+              q_held = false;
+            }
+            ++gs;
+            cs.next();
+            progressed = true;
           }
-          if (t > t0) {
-            // weighted sums of the previous tile
-            const int64_t gw = g - 1;
-            const int64_t pos = (t - 1 - t0) % S_GROUP;
-            const bool first = pos == 0;
-            const bool last = pos == S_GROUP - 1 || t == t1;
-            const int par = (int)(grp & 1);
-            const int sw = (int)(gw % SNS);
-            if (first && !mbar_wait(&wempty[par], (uint32_t)(((grp >> 1) & 1) ^ 1), 26)) goto done;
-            const uint32_t bs = smem_u32(sB + sw * S_STAGE_BYTES);
+        }
+        {
+          // weighted sums of tile gw
+          const int b = gw % NBUF;
+          const int s = gw % SNS;
+          const int pos = (cw.t - cw.t0) % S_GROUP;
+          const bool first = pos == 0;
+          const bool last = pos == S_GROUP - 1 || cw.t == cw.t1 - 1;
+          const int par = grp & 1;
+          bool ready = gw < gs;
+          if (ready && first) ready = mbar_try_wait(&wempty[par], (uint32_t)(((grp >> 1) & 1) ^ 1));
+#pragma unroll
+          for (int a = 0; a < SNQT; ++a)
+            if (ready) ready = mbar_try_wait(&pready[b * SNQT + a], (uint32_t)((gw / NBUF) & 1));
+          if (ready) {
+            tc_fence_after();
+            const uint32_t bs = smem_u32(sB + s * S_STAGE_BYTES);
 #pragma unroll
             for (int a = 0; a < SNQT; ++a) {
-              if (!mbar_wait(&pready[a], (uint32_t)(gw & 1), 27)) goto done;
-              tc_fence_after();
-              const uint32_t d = tmem_base + (uint32_t)(T_W + par * (SNQT * FSK_D) + a * FSK_D);
-              const uint32_t ph = tmem_base + (uint32_t)(T_PHI + a * NT);
+              const uint32_t d = tmem_base + (uint32_t)(T_W + par * (SNQT * WN) + a * WN);
+              const uint32_t ph = tmem_base + (uint32_t)(T_S + b * (SNQT * NT) + a * NT);
 #pragma unroll
               for (int ks = 0; ks < NT / 16; ++ks) {
-                const uint64_t xh = smem_desc_kmajor(bs + S_XTH_OFFSET + 256 * ks, 128, 8 * XT_ROW_BYTES);
-                const uint64_t xl = smem_desc_kmajor(bs + S_XTL_OFFSET + 256 * ks, 128, 8 * XT_ROW_BYTES);
-                mma_f16_ts(d, ph + 8 * ks, xh, idesc_w, (first && ks == 0) ? 0u : 1u);
-                mma_f16_ts(d, ph + 8 * ks, xl, idesc_w, 1u);
-                mma_f16_ts(d, ph + NT / 2 + 8 * ks, xh, idesc_w, 1u);
+                // data columns 16 ks .. +15: column half ks/2, weights hi at +0, lo at +16
+                const uint32_t wa = ph + (uint32_t)(32 * (ks >> 1) + 8 * (ks & 1));
+                const uint64_t xd = smem_desc_kmajor(bs + S_XTH_OFFSET + 256 * ks, 128, 8 * XT_ROW_BYTES);
+                mma_f16_ts(d, wa, xd, idesc_w, (first && ks == 0) ? 0u : 1u);
+                mma_f16_ts(d, wa + 16, xd, idesc_w, 1u);
               }
-              mma_commit(&pfree[a]);
             }
-            mma_commit(&empty[sw]);
+            mma_commit(&wdone[b]);
+            mma_commit(&empty[s]);
             if (last) {
               mma_commit(&wfull[par]);
               ++grp;
             }
+            ++gw;
+            cw.next();
+            progressed = true;
           }
-          if (t < t1) ++g;
+        }
+        if (progressed) {
+          idle_since = 0;
+        } else {
+          const uint64_t now = globaltimer_ns();
+          if (idle_since == 0) {
+            idle_since = now;
+          } else if (now - idle_since > 2000000000ull) {
+            record_error(FSK_ERR_DEVICE_TIMEOUT, 23);
+            goto done;
+          }
         }
       }
     }
@@ -258,9 +342,6 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
     const float out_mul = p.scales->out_mul;
     const bool scaled = out_mul != 1.0f;
     const float phi_scale = 32768.0f;     // 2^PHI_LOG2_SCALE
-    const double w_unscale = ldexp(1.0, -(int)PHI_LOG2_SCALE - p.scales->pad[2]);
-    const double p_unscale = ldexp(1.0, -(int)PHI_LOG2_SCALE);
-    const double c_unscale = ldexp(1.0, -(int)PHI_LOG2_SCALE);
     // correction rows: wcorr[parity][half][qt*128 + row][16]
     const int wc_row = (qt * QT + row) * FSK_D;
     constexpr int WC_HALF = SNQT * QT * FSK_D, WC_PAR = 2 * WC_HALF;
@@ -285,25 +366,24 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
       float* wc = wcorr + (k_unit & 1) * WC_PAR + half * WC_HALF + wc_row;
       Comp acc{0.f, 0.f};
       float corr = 0.f;
-      Comp wacc[FSK_D / 2];
+      constexpr int EPI_T = S_EPI_WARPS * 32;
 #pragma unroll
-      for (int k = 0; k < FSK_D / 2; ++k) wacc[k] = Comp{0.f, 0.f};
+      for (int k = 0; k < 4; ++k) wacc[k * EPI_T + threadIdx.x] = make_float4(0.f, 0.f, 0.f, 0.f);
       const int t0 = sp * tps;
       const int t1 = imin(n_tiles, t0 + tps);
       bool pend = false;     // a W group ended at the previous tile and is not read yet
       for (int t = t0; t < t1; ++t, ++g) {
         const int s = g % SNS;
-        const int b = g & 1;
+        const int b = g % NBUF;
         const int valid = (int)imin<int64_t>(NT, p.n - (int64_t)t * NT);
-        if (!mbar_wait(&tfull[b], (uint32_t)((g >> 1) & 1), 28)) goto done;
+        if (!mbar_wait(&tfull[b], (uint32_t)((g / NBUF) & 1), 28)) goto done;
         tc_fence_after();
         const uint8_t* stage = sB + s * S_STAGE_BYTES;
+        // this warp's 32 S columns; its weights go back into the same columns
+        const uint32_t my_cols = tmem_base + lane_off + (uint32_t)(T_S + b * (SNQT * NT) + qt * NT + half * 32);
         uint32_t r[32];
-        tmem_ld32(tmem_base + lane_off + (uint32_t)(T_S + b * (SNQT * NT) + qt * NT + half * 32), r);
+        tmem_ld32(my_cols, r);
         tmem_ld_wait();
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&tempty[b]);
         float e[32];
         if (scaled) {
 #pragma unroll
@@ -341,34 +421,41 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
           // (corr) and the weighted sum (ex - A)(x_j - mu) (shared-memory
           // corrections), so both see the same weight e_j - A + ex.
           if (trig) {
-            uint32_t key[16];
+            // four interleaved max chains keep the register peak low
+            uint32_t k0 = 0u, k1 = 0u, k2 = 0u, k3 = 0u;
 #pragma unroll
-            for (int j = 0; j < 16; ++j)
-              key[j] = max((__float_as_uint(e[j]) & ~31u) | (uint32_t)j,
-                           (__float_as_uint(e[j + 16]) & ~31u) | (uint32_t)(j + 16));
-#pragma unroll
-            for (int w = 8; w >= 1; w >>= 1)
-#pragma unroll
-              for (int j = 0; j < w; ++j) key[j] = max(key[j], key[j + w]);
-            const uint32_t kmax = key[0];
-            const int j = (int)(kmax & 31u);
-            float qx[FSK_D];   // the query's original coordinates (L1-resident after first use)
-#pragma unroll
-            for (int kk = 0; kk < FSK_D; kk += 4) {
-              const float4 v = __ldg(reinterpret_cast<const float4*>(p.qexact + (int64_t)gi * FSK_D + kk));
-              qx[kk] = v.x; qx[kk + 1] = v.y; qx[kk + 2] = v.z; qx[kk + 3] = v.w;
+            for (int j = 0; j < 32; j += 4) {
+              k0 = max(k0, (__float_as_uint(e[j]) & ~31u) | (uint32_t)j);
+              k1 = max(k1, (__float_as_uint(e[j + 1]) & ~31u) | (uint32_t)(j + 1));
+              k2 = max(k2, (__float_as_uint(e[j + 2]) & ~31u) | (uint32_t)(j + 2));
+              k3 = max(k3, (__float_as_uint(e[j + 3]) & ~31u) | (uint32_t)(j + 3));
             }
+            const uint32_t kmax = max(max(k0, k1), max(k2, k3));
+            const int j = (int)(kmax & 31u);
             const int col = half * 32 + j;
-            const float dist = exact_dist(stage, col, qx, S_X_OFFSET);
+            const float4* xr = reinterpret_cast<const float4*>(stage + S_X_OFFSET + col * (FSK_D * 4));
+            // exact squared distance, four features at a time (query from
+            // its original coordinates, L1-resident after first use)
+            const float4* qr = reinterpret_cast<const float4*>(sQ + (qt * QT + row) * FSK_D);
+            float d0 = 0.f, d1 = 0.f, d2 = 0.f, d3 = 0.f;
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+              const float4 qv = qr[kk], xv = xr[kk];
+              const float a0 = qv.x - xv.x, a1 = qv.y - xv.y, a2 = qv.z - xv.z, a3 = qv.w - xv.w;
+              d0 = fmaf(a0, a0, d0);
+              d1 = fmaf(a1, a1, d1);
+              d2 = fmaf(a2, a2, d2);
+              d3 = fmaf(a3, a3, d3);
+            }
+            const float dist = (d0 + d1) + (d2 + d3);
             float ex = exp2_neg_scaled(dist, p.c2, p.c2_lo) * phi_scale;
             if (col >= valid || t * NT + col == gi) ex = 0.f;
             const float delta = ex - __uint_as_float(kmax);
             corr += delta;
-            const float4* xr = reinterpret_cast<const float4*>(stage + S_X_OFFSET + col * (FSK_D * 4));
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk) {
               const float4 xv = xr[kk];
-              const float4 mv = __ldg(reinterpret_cast<const float4*>(p.mu) + kk);
+              const float4 mv = reinterpret_cast<const float4*>(sMu)[kk];
               float4 cv = *reinterpret_cast<float4*>(wc + 4 * kk);
               cv.x = fmaf(delta, xv.x - mv.x, cv.x);
               cv.y = fmaf(delta, xv.y - mv.y, cv.y);
@@ -380,20 +467,18 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
           __syncwarp();
         }
         acc.add(cs);
-        // fp16 hi / lo weights for the W product; the previous tile's W MMA
-        // must have finished reading this query tile's weight columns.
+        // fp16 hi / lo weights for the W product, written over this warp's
+        // S columns (hi: 16 columns of packed pairs, then lo)
         uint32_t hi[16], lo[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) split_pack(e[2 * j], e[2 * j + 1], hi[j], lo[j]);
-        if (g > 0 && !mbar_wait(&pfree[qt], (uint32_t)((g - 1) & 1), 29)) goto done;
-        tc_fence_after();
-        tmem_st16(tmem_base + lane_off + (uint32_t)(T_PHI + qt * NT + half * 16), hi);
-        tmem_st16(tmem_base + lane_off + (uint32_t)(T_PHI + qt * NT + NT / 2 + half * 16), lo);
+        tmem_st16(my_cols, hi);
+        tmem_st16(my_cols + 16, lo);
         tmem_st_wait();
         tc_fence_before();
         __syncwarp();
         if (lane == 0) {
-          mbar_arrive(&pready[qt]);
+          mbar_arrive(&pready[b * SNQT + qt]);
           mbar_arrive(&empty[s]);
         }
         // read a W group that ended at the previous tile (its MMAs were
@@ -406,14 +491,31 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
           const int par = grp & 1;
           if (!mbar_wait(&wfull[par], (uint32_t)((grp >> 1) & 1), 30)) goto done;
           tc_fence_after();
-          uint32_t wv[8];
-          tmem_ld8(tmem_base + lane_off + (uint32_t)(T_W + par * (SNQT * FSK_D) + qt * FSK_D + half * 8), wv);
+          uint32_t wv[8], wl[8];   // X_hi and X_lo parts of this warp's 8 features
+          const uint32_t wcol = tmem_base + lane_off + (uint32_t)(T_W + par * (SNQT * WN) + qt * WN + half * 8);
+          tmem_ld8(wcol, wv);
+          tmem_ld8(wcol + FSK_D, wl);
           tmem_ld_wait();
+#pragma unroll
+          for (int k = 0; k < 8; ++k) wv[k] = __float_as_uint(__uint_as_float(wv[k]) + __uint_as_float(wl[k]));
           tc_fence_before();
           __syncwarp();
           if (lane == 0) mbar_arrive(&wempty[par]);
-#pragma unroll
-          for (int k = 0; k < 8; ++k) wacc[k].add(__uint_as_float(wv[k]));
+          {
+            float4 s0 = wacc[threadIdx.x], s1 = wacc[EPI_T + threadIdx.x];
+            float4 e0 = wacc[2 * EPI_T + threadIdx.x], e1 = wacc[3 * EPI_T + threadIdx.x];
+            Comp c;
+#define FSK_WADD(S, E, V) c = Comp{S, E}; c.add(__uint_as_float(V)); S = c.s; E = c.c;
+            FSK_WADD(s0.x, e0.x, wv[0]) FSK_WADD(s0.y, e0.y, wv[1])
+            FSK_WADD(s0.z, e0.z, wv[2]) FSK_WADD(s0.w, e0.w, wv[3])
+            FSK_WADD(s1.x, e1.x, wv[4]) FSK_WADD(s1.y, e1.y, wv[5])
+            FSK_WADD(s1.z, e1.z, wv[6]) FSK_WADD(s1.w, e1.w, wv[7])
+#undef FSK_WADD
+            wacc[threadIdx.x] = s0;
+            wacc[EPI_T + threadIdx.x] = s1;
+            wacc[2 * EPI_T + threadIdx.x] = e0;
+            wacc[3 * EPI_T + threadIdx.x] = e1;
+          }
           ++grp;
           if (pass == 0) pend = false;
         }
@@ -425,7 +527,10 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
       // previous parity is cleared once every warp has passed this unit's
       // barrier (so has finished reading it).
       __syncwarp();
-      if (lane == 0) mbar_arrive(cready);
+      if (lane == 0) {
+        mbar_arrive(cready);
+        mbar_arrive(qempty);   // done with this unit's query rows in shared memory
+      }
       if (!mbar_wait(cready, (uint32_t)(k_unit & 1), 35)) goto done;
       {
         float* wc_next = wcorr + ((k_unit + 1) & 1) * WC_PAR + half * WC_HALF + wc_row;
@@ -434,14 +539,20 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
           *reinterpret_cast<float4*>(wc_next + k) = make_float4(0.f, 0.f, 0.f, 0.f);
       }
       if (gi < p.n) {
+        const double p_unscale = 1.0 / 32768.0;   // 2^-PHI_LOG2_SCALE
+        const double c_unscale = p_unscale;
+        const double w_unscale = ldexp(p_unscale, -p.scales->pad[2]);
         p.ppdf[(int64_t)(2 * sp + half) * p.n + gi] = ((double)acc.s + (double)acc.c + (double)corr) * p_unscale;
         double* wrow = p.pw + ((int64_t)sp * p.n + gi) * FSK_D + half * 8;
         const float* c0 = wcorr + (k_unit & 1) * WC_PAR + wc_row + half * 8;
         const float* c1 = c0 + WC_HALF;
+        const float4 s0 = wacc[threadIdx.x], s1 = wacc[EPI_T + threadIdx.x];
+        const float4 e0 = wacc[2 * EPI_T + threadIdx.x], e1 = wacc[3 * EPI_T + threadIdx.x];
+        const float ws[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
+        const float we[8] = {e0.x, e0.y, e0.z, e0.w, e1.x, e1.y, e1.z, e1.w};
 #pragma unroll
         for (int k = 0; k < 8; ++k)
-          wrow[k] = ((double)wacc[k].s + (double)wacc[k].c) * w_unscale +
-                    ((double)c0[k] + (double)c1[k]) * c_unscale;
+          wrow[k] = ((double)ws[k] + (double)we[k]) * w_unscale + ((double)c0[k] + (double)c1[k]) * c_unscale;
       }
     }
   }
