@@ -26,12 +26,13 @@
 //    from the data stage, N = 32, FP32 accumulation over a group of S_GROUP
 //    tiles, then added into compensated FP32 sums.
 //
-// Pipeline (one persistent CTA per SM, 18 warps):
+// Pipeline (one persistent CTA per SM, 19 warps):
 //   warp 16 : producer (bulk copies of query images per unit, data stages).
 //   warp 17 : owns TMEM; issues S up to NBUF tiles ahead of W (one lane).
-//             An M=128, K=16 tcgen05.mma costs ~46 cycles whatever N <= 64
-//             is, so the weighted-sum product is the expensive part: two
-//             N=32 MMAs per K step, and the epilogue never waits for it.
+//   warp 18 : issues the weighted-sum MMAs (one lane).  An M=128, K=16
+//             tcgen05.mma costs ~46 cycles whatever N <= 64 is, so this
+//             product is the expensive part: two N=32 MMAs per K step, and
+//             the epilogue never waits for it.
 //   warps 0-15: epilogue; warp w: query tile w/8, data-column half (w/4)&1,
 //             TMEM lane quarter w&3.  The two column halves of a row keep
 //             separate pdf partials (written as two virtual splits) and
@@ -60,8 +61,9 @@ constexpr int S_STAGE_BYTES = S_X_OFFSET + NT * FSK_D * 4; // 14 KB
 constexpr int S_A_BYTES = SNQT * A_TILE_BYTES;             // 24 KB
 constexpr int S_EPI_WARPS = 8 * SNQT;
 constexpr int S_PRODUCER_WARP = S_EPI_WARPS;
-constexpr int S_MMA_WARP = S_EPI_WARPS + 1;
-constexpr int S_THREADS = (S_EPI_WARPS + 2) * 32;
+constexpr int S_MMA_WARP = S_EPI_WARPS + 1;     // issues the S MMAs, owns TMEM
+constexpr int W_MMA_WARP = S_EPI_WARPS + 2;     // issues the weighted-sum MMAs
+constexpr int S_THREADS = (S_EPI_WARPS + 3) * 32;
 constexpr int S_GROUP = 8;                                 // data tiles per W accumulation
 constexpr int NBUF = 3;                                    // S / weight buffers in TMEM
 constexpr int WN = 2 * FSK_D;                              // W MMA N: X_hi and X_lo rows
@@ -146,7 +148,6 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
   uint64_t* full = bars;                      // [SNS] stage loaded
   uint64_t* empty = bars + SNS;               // [SNS] stage consumed (W MMA + epilogue)
   uint64_t* tfull = bars + 2 * SNS;           // [NBUF] S buffer written
-  uint64_t* wdone = bars + 2 * SNS + 3;       // [NBUF] W MMA done reading the buffer's weights
   // [NBUF][SNQT] weights of a query tile stored in a buffer.  One barrier per
   // buffer: the epilogue may run NBUF tiles ahead of the W MMA, and a
   // buffer's barrier cannot complete again before its weights are consumed.
@@ -170,10 +171,7 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1 + S_EPI_WARPS);
     }
-    for (int b = 0; b < NBUF; ++b) {
-      mbar_init(&tfull[b], 1);
-      mbar_init(&wdone[b], 1);
-    }
+    for (int b = 0; b < NBUF; ++b) mbar_init(&tfull[b], 1);
     for (int b = 0; b < 2; ++b) {
       mbar_init(&wfull[b], 1);
       mbar_init(&wempty[b], S_EPI_WARPS);
@@ -181,7 +179,7 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
     for (int i = 0; i < NBUF * SNQT; ++i) mbar_init(&pready[i], 8);
     mbar_init(qready, 1);
     mbar_init(qempty, 1 + S_EPI_WARPS);   // last S MMA of the unit + every epilogue warp
-    mbar_init(drain, 1);
+    mbar_init(drain, 2);
     mbar_init(cready, S_EPI_WARPS);
     fence_barrier_init();
   }
@@ -221,112 +219,98 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
       }
     }
   } else if (warp == S_MMA_WARP) {
+    // S(g) for every tile, up to NBUF tiles ahead of the W MMAs: buffer
+    // g % NBUF is reused once W(g - NBUF) has read its weights, which the
+    // stage barrier of tile g - NBUF signals (it completes with the W
+    // thread's commit; that tile's epilogue arrivals came earlier).  S and W
+    // are issued by different threads because tcgen05.commit tracks every
+    // earlier MMA of its thread: waiting for W(g - NBUF) from one issuing
+    // thread would also wait for the S MMAs issued after it and drain the
+    // tensor pipe every tile.
     if (lane == 0) {
       const uint32_t idesc_s = idesc_f16_f32(QT, NT);
-      const uint32_t idesc_w = idesc_f16_f32(QT, WN);
-      // Two cursors over this CTA's tiles: S runs up to NBUF tiles ahead of W.
-      // Nothing here blocks: each pass issues S and/or W when all their
-      // barriers have completed (the next unit's query images, for instance,
-      // arrive only after the epilogue has read this unit's last W group, so
-      // waiting for them before issuing that W would deadlock).  One watchdog
-      // bounds the time without progress.
-      TileCursor cs, cw;
+      uint64_t a_hf[SNQT], a_hb[SNQT], a_l[SNQT];
+#pragma unroll
+      for (int a = 0; a < SNQT; ++a) {
+        const uint32_t as = smem_u32(sA + a * A_TILE_BYTES);
+        a_hf[a] = smem_desc_kmajor(as, 128, 8 * H_ROW_BYTES);
+        a_hb[a] = a_hf[a] + (256 >> 4);   // bias K step (start-address field, no carry below 2^18 B)
+        a_l[a] = smem_desc_kmajor(as + A_H_BYTES, 128, 8 * L_ROW_BYTES);
+      }
+      const uint32_t b0 = smem_u32(sB);
+      const uint64_t dh0 = smem_desc_kmajor(b0, 128, 8 * H_ROW_BYTES);
+      const uint64_t dl0 = smem_desc_kmajor(b0 + B_H_BYTES, 128, 8 * L_ROW_BYTES);
+      TileCursor cs;
       cs.start((int)u_begin, (int)u_end, (int)p.splits, (int)p.tiles_per_split, (int)p.n_tiles);
-      cw = cs;
-      int gs = 0, gw = 0, kq = 0, grp = 0;
-      bool q_held = false;   // query images of the S cursor's unit are resident
-      uint64_t idle_since = 0;
+      int gs = 0, kq = 0;
+      while (!cs.done()) {
+        const int s = gs % SNS;
+        if (cs.t == cs.t0) {   // first tile of a unit: its query images
+          if (!mbar_wait(qready, (uint32_t)(kq & 1), 23)) goto done;
+          ++kq;
+        }
+        const int gp = gs - NBUF;
+        if (gp >= 0 && !mbar_wait(&empty[gp % SNS], (uint32_t)((gp / SNS) & 1), 25)) goto done;
+        if (!mbar_wait(&full[s], (uint32_t)((gs / SNS) & 1), 24)) goto done;
+        tc_fence_after();
+        const uint64_t so = (uint64_t)((s * S_STAGE_BYTES) >> 4);
+        const uint64_t b_hf = dh0 + so, b_hb = dh0 + so + (256 >> 4), b_l = dl0 + so;
+        const uint32_t d0 = tmem_base + (uint32_t)(T_S + (gs % NBUF) * (SNQT * NT));
+#pragma unroll
+        for (int a = 0; a < SNQT; ++a) {
+          const uint32_t d = d0 + (uint32_t)(a * NT);
+          mma_f16_ss(d, a_l[a], b_hf, idesc_s, 0u);
+          mma_f16_ss(d, a_hf[a], b_l, idesc_s, 1u);
+          mma_f16_ss(d, a_hf[a], b_hf, idesc_s, 1u);
+          mma_f16_ss(d, a_hb[a], b_hb, idesc_s, 1u);
+        }
+        mma_commit(&tfull[gs % NBUF]);
+        if (cs.t == cs.t1 - 1) mma_commit(qempty);   // last S read of this unit's query images
+        ++gs;
+        cs.next();
+      }
+    }
+  } else if (warp == W_MMA_WARP) {
+    // W(g) once the epilogue has stored tile g's weights (both query tiles).
+    if (lane == 0) {
+      const uint32_t idesc_w = idesc_f16_f32(QT, WN);
+      const uint64_t dx0 = smem_desc_kmajor(smem_u32(sB) + S_XTH_OFFSET, 128, 8 * XT_ROW_BYTES);
+      TileCursor cw;
+      cw.start((int)u_begin, (int)u_end, (int)p.splits, (int)p.tiles_per_split, (int)p.n_tiles);
+      int gw = 0, grp = 0;
       while (!cw.done()) {
-        bool progressed = false;
-        if (!cs.done() && gs < gw + NBUF) {
-          const int b = gs % NBUF;
-          const int s = gs % SNS;
-          if (cs.t == cs.t0 && !q_held && mbar_try_wait(qready, (uint32_t)(kq & 1))) {
-            q_held = true;
-            ++kq;
-          }
-          // the buffer's previous weights (tile gs - NBUF) must be consumed
-          if ((cs.t != cs.t0 || q_held) &&
-              (gs < NBUF || mbar_try_wait(&wdone[b], (uint32_t)(((gs - NBUF) / NBUF) & 1))) &&
-              mbar_try_wait(&full[s], (uint32_t)((gs / SNS) & 1))) {
-            tc_fence_after();
-            const uint32_t bs = smem_u32(sB + s * S_STAGE_BYTES);
-            const uint64_t b_hf = smem_desc_kmajor(bs, 128, 8 * H_ROW_BYTES);
-            const uint64_t b_hb = smem_desc_kmajor(bs + 256, 128, 8 * H_ROW_BYTES);
-            const uint64_t b_l = smem_desc_kmajor(bs + B_H_BYTES, 128, 8 * L_ROW_BYTES);
+        const int b = gw % NBUF;
+        const int s = gw % SNS;
+        const int pos = (cw.t - cw.t0) % S_GROUP;
+        const bool first = pos == 0;
+        const bool last = pos == S_GROUP - 1 || cw.t == cw.t1 - 1;
+        const int par = grp & 1;
+        if (first && !mbar_wait(&wempty[par], (uint32_t)(((grp >> 1) & 1) ^ 1), 26)) goto done;
 #pragma unroll
-            for (int a = 0; a < SNQT; ++a) {
-              const uint32_t as = smem_u32(sA + a * A_TILE_BYTES);
-              const uint64_t a_hf = smem_desc_kmajor(as, 128, 8 * H_ROW_BYTES);
-              const uint64_t a_hb = smem_desc_kmajor(as + 256, 128, 8 * H_ROW_BYTES);
-              const uint64_t a_l = smem_desc_kmajor(as + A_H_BYTES, 128, 8 * L_ROW_BYTES);
-              const uint32_t d = tmem_base + (uint32_t)(T_S + b * (SNQT * NT) + a * NT);
-              mma_f16_ss(d, a_l, b_hf, idesc_s, 0u);
-              mma_f16_ss(d, a_hf, b_l, idesc_s, 1u);
-              mma_f16_ss(d, a_hf, b_hf, idesc_s, 1u);
-              mma_f16_ss(d, a_hb, b_hb, idesc_s, 1u);
-            }
-            mma_commit(&tfull[b]);
-            if (cs.t == cs.t1 - 1) {
-              mma_commit(qempty);   // last S read of this unit's query images
-              q_held = false;
-            }
-            ++gs;
-            cs.next();
-            progressed = true;
+        for (int a = 0; a < SNQT; ++a)
+          if (!mbar_wait(&pready[b * SNQT + a], (uint32_t)((gw / NBUF) & 1), 27)) goto done;
+        tc_fence_after();
+        const uint64_t xd0 = dx0 + (uint64_t)((s * S_STAGE_BYTES) >> 4);
+        const uint32_t ph0 = tmem_base + (uint32_t)(T_S + b * (SNQT * NT));
+        const uint32_t d0 = tmem_base + (uint32_t)(T_W + par * (SNQT * WN));
+#pragma unroll
+        for (int a = 0; a < SNQT; ++a) {
+#pragma unroll
+          for (int ks = 0; ks < NT / 16; ++ks) {
+            // data columns 16 ks .. +15: column half ks/2, weights hi at +0, lo at +16
+            const uint32_t wa = ph0 + (uint32_t)(a * NT + 32 * (ks >> 1) + 8 * (ks & 1));
+            const uint64_t xd = xd0 + (uint64_t)(ks * (256 >> 4));
+            mma_f16_ts(d0 + (uint32_t)(a * WN), wa, xd, idesc_w, (first && ks == 0) ? 0u : 1u);
+            mma_f16_ts(d0 + (uint32_t)(a * WN), wa + 16, xd, idesc_w, 1u);
           }
         }
-        {
-          // weighted sums of tile gw
-          const int b = gw % NBUF;
-          const int s = gw % SNS;
-          const int pos = (cw.t - cw.t0) % S_GROUP;
-          const bool first = pos == 0;
-          const bool last = pos == S_GROUP - 1 || cw.t == cw.t1 - 1;
-          const int par = grp & 1;
-          bool ready = gw < gs;
-          if (ready && first) ready = mbar_try_wait(&wempty[par], (uint32_t)(((grp >> 1) & 1) ^ 1));
-#pragma unroll
-          for (int a = 0; a < SNQT; ++a)
-            if (ready) ready = mbar_try_wait(&pready[b * SNQT + a], (uint32_t)((gw / NBUF) & 1));
-          if (ready) {
-            tc_fence_after();
-            const uint32_t bs = smem_u32(sB + s * S_STAGE_BYTES);
-#pragma unroll
-            for (int a = 0; a < SNQT; ++a) {
-              const uint32_t d = tmem_base + (uint32_t)(T_W + par * (SNQT * WN) + a * WN);
-              const uint32_t ph = tmem_base + (uint32_t)(T_S + b * (SNQT * NT) + a * NT);
-#pragma unroll
-              for (int ks = 0; ks < NT / 16; ++ks) {
-                // data columns 16 ks .. +15: column half ks/2, weights hi at +0, lo at +16
-                const uint32_t wa = ph + (uint32_t)(32 * (ks >> 1) + 8 * (ks & 1));
-                const uint64_t xd = smem_desc_kmajor(bs + S_XTH_OFFSET + 256 * ks, 128, 8 * XT_ROW_BYTES);
-                mma_f16_ts(d, wa, xd, idesc_w, (first && ks == 0) ? 0u : 1u);
-                mma_f16_ts(d, wa + 16, xd, idesc_w, 1u);
-              }
-            }
-            mma_commit(&wdone[b]);
-            mma_commit(&empty[s]);
-            if (last) {
-              mma_commit(&wfull[par]);
-              ++grp;
-            }
-            ++gw;
-            cw.next();
-            progressed = true;
-          }
+        mma_commit(&empty[s]);
+        if (last) {
+          mma_commit(&wfull[par]);
+          ++grp;
         }
-        if (progressed) {
-          idle_since = 0;
-        } else {
-          const uint64_t now = globaltimer_ns();
-          if (idle_since == 0) {
-            idle_since = now;
-          } else if (now - idle_since > 2000000000ull) {
-            record_error(FSK_ERR_DEVICE_TIMEOUT, 23);
-            goto done;
-          }
-        }
+        ++gw;
+        cw.next();
       }
     }
   } else {
@@ -564,8 +548,8 @@ done:
       mbar_wait(&full[i % SNS], (uint32_t)((i / SNS) & 1), 32);
     if (n_query_copies > 0) mbar_wait(qready, (uint32_t)((n_query_copies - 1) & 1), 33);
   }
-  if (warp == S_MMA_WARP && lane == 0) {
-    mma_commit(drain);
+  if ((warp == S_MMA_WARP || warp == W_MMA_WARP) && lane == 0) {
+    mma_commit(drain);   // one arrival per issuing thread, when its MMAs have finished
     mbar_wait(drain, 0, 34);
   }
   tc_fence_before();
