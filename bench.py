@@ -49,13 +49,17 @@ K_OPS_PER_POLY_EXP = 10.0
 KERNEL_NAMES = {1: "kde16_tc_kernel", 2: "kde16_simt_kernel", 3: "score16_simt_kernel",
                 4: "score16_sym_simt_kernel", 5: "kde1d_kernel", 6: "kde1d_score_kernel",
                 7: "score16_tc_kernel"}
+# fp16 tensor-core flops per pair evaluation issued by the tcgen05 kernels:
+# KDE: 4 MMAs (M=128, N=64, K=16) per 128x64 pairs; score: the same S
+# product plus 16 MMAs (M=128, N=32, K=16) per 256x64 pairs.
+MMA_FLOPS_PER_PAIR = {"kde16_tc_kernel": 4 * 2 * 16, "score16_tc_kernel": 4 * 2 * 16 + 16 * 2 * 128 * 32 * 16 / (256 * 64)}
 
 
 def parse():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["fsk", "reference"], default="fsk")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--op", choices=["kde16", "score16"], default=None,
@@ -138,7 +142,7 @@ def run_reference_arm(args) -> None:
 # GPU arm
 # ---------------------------------------------------------------------------
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks / throttle reasons sampled every 100 ms."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -154,7 +158,7 @@ class ClockSampler:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+                 "-lms", "100"], stdout=self.fh, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
@@ -198,6 +202,21 @@ def exp_peak(rates) -> dict:
     f = (r_fma - c * r_sfu) / (r_fma + k * r_sfu)
     peak = r_sfu / (1.0 - f) if f > 0 else min(r_sfu, r_fma / c)
     return {"peak": peak, "r_sfu": r_sfu, "r_fma": r_fma, "r_ffma2_lanes": float(rates[2]), "offload_fraction": max(f, 0.0)}
+
+
+def tensor_roofline(kernel, pairs_per_s) -> dict | None:
+    """Tensor-pipe view of the dominant kernel: its fp16 MMA flops per second
+    against the measured dense bf16 peak (same tensor rate as fp16)."""
+    if not kernel or kernel not in MMA_FLOPS_PER_PAIR or not pairs_per_s:
+        return None
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("bf16_tflops")
+    src = "MEASURED_PEAKS.json bf16_tflops (burst, cuBLAS)"
+    if not peak:
+        peak, src = 1900.0, "fallback 1.9 PFLOP/s"
+    achieved = pairs_per_s * MMA_FLOPS_PER_PAIR[kernel] / 1e12
+    return {"bound": "tensor", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "flops_per_pair": MMA_FLOPS_PER_PAIR[kernel], "peak_source": src}
 
 
 def run_gpu_arm(args) -> None:
@@ -371,6 +390,7 @@ def run_gpu_arm(args) -> None:
                                         "(fsk_diag_pipe_rates); P = R_sfu/(1-f*), c=%g, k=%g"
                                         % (peak["r_sfu"], peak["r_fma"], C_OPS_PER_PAIR, K_OPS_PER_POLY_EXP),
                          "sfu_only_peak": peak["r_sfu"]},
+            "roofline_tensor": tensor_roofline(dom, achieved),
             "kernels": kernels,
             "cpu_baseline": cpu,
             "clocks": sampler.summary(),
