@@ -62,6 +62,12 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["fsk", "reference"], default="fsk")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--surrogate", action="store_true",
+                    help="run only the learned-surrogate workload (C4) and print its JSON line")
+    ap.add_argument("--no-surrogate", action="store_true", help="leave the surrogate object out of the bench line")
+    ap.add_argument("--sur-train", type=int, default=262144, help="surrogate workload: exact SD-KDE fit points")
+    ap.add_argument("--sur-pairs", type=int, default=4_000_000, help="surrogate workload: training pairs")
+    ap.add_argument("--sur-eval", type=int, default=1_000_000, help="surrogate workload: held-out queries")
     ap.add_argument("--op", choices=["kde16", "score16"], default=None,
                     help="time one operation alone on n GMM8 points (profiling case; no contract line)")
     ap.add_argument("--n", type=int, default=N_TRAIN, help="points for --op (queries = data)")
@@ -403,6 +409,86 @@ def run_gpu_arm(args) -> None:
         dist.destroy_process_group()
 
 
+def surrogate_workload(args, dev) -> dict:
+    """Learned surrogate (C4): exact SD-KDE fit on n GMM8 points, ensemble of
+    4 MLPs trained on (data + N(0, h^2 I), exact log p) pairs, evaluated on
+    held-out queries, half in-support (same recipe, new seed) and half
+    N(0, 9 I).  Reports the gated path (surrogate + exact fallback), the
+    surrogate alone and the exact KDE in queries/s, with the median relative
+    density error over the served queries and the fallback rate."""
+    import torch
+
+    from flash_sd_kde import emp_sd_kde_fit_transform
+    from flash_sd_kde.surrogate import SurrogateKDE
+    from fsk import ops, workloads
+
+    gmm = workloads.GMM16(seed=0)
+    x = torch.from_numpy(gmm.sample(args.sur_train, seed=1)).to(dev)
+    h = float(ops.silverman(x).item())
+    deb = emp_sd_kde_fit_transform(x, h, device=dev)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    sur = SurrogateKDE(members=4).fit(deb, h, n_pairs=args.sur_pairs)
+    torch.cuda.synchronize(dev)
+    fit_s = time.perf_counter() - t0
+    g = torch.Generator(device=dev).manual_seed(12345)
+    half = args.sur_eval // 2
+    idx = torch.randint(deb.shape[0], (half,), generator=g, device=dev)
+    q_in = deb[idx] + torch.randn((half, 16), generator=g, device=dev) * h
+    q_out = torch.randn((args.sur_eval - half, 16), generator=g, device=dev) * 3.0
+    q = torch.cat([q_in, q_out]).contiguous()
+
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            out = fn()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / reps, out
+
+    ms_exact, exact = timed(lambda: sur._exact_logp(q))
+    ms_gated, (logp, served) = timed(lambda: sur.score_samples(q, return_served=True))
+    ms_sur, _ = timed(lambda: sur.predict(q))
+    ops.device_status(dev)
+    fin = torch.isfinite(exact)          # far queries can underflow the FP32 kernel sum (log 0)
+    rel = (torch.exp((logp - exact).double()) - 1).abs()
+    srv = served.bool() & fin
+    n = q.shape[0]
+    return {
+        "workload": f"surrogate_gmm8_16d_fit{args.sur_train}_pairs{args.sur_pairs}_eval{n}",
+        "members": 4, "mlp": "16-256-256-256-1 SiLU, bf16 weights/activations, FP32 accumulation",
+        "fit_seconds": fit_s, "train_mse_normalised": sur.history[-1] if sur.history else None,
+        "exact_queries_per_s": n / (ms_exact * 1e-3),
+        "gated_queries_per_s": n / (ms_gated * 1e-3),
+        "surrogate_only_queries_per_s": n / (ms_sur * 1e-3),
+        "speedup_gated_vs_exact": ms_exact / ms_gated,
+        "speedup_surrogate_only_vs_exact": ms_exact / ms_sur,
+        "served_fraction": float(srv.float().mean()),
+        "served_fraction_in_support": float(srv[:half].float().mean()),
+        "served_fraction_out_of_support": float(srv[half:].float().mean()),
+        "median_rel_density_err_served": float(rel[srv].median()) if srv.any() else None,
+        "p90_rel_density_err_served": float(torch.quantile(rel[srv].float(), 0.9)) if srv.any() else None,
+        "median_rel_density_err_all_surrogate": float(
+            (torch.exp((sur.predict(q)[0] - exact).double()) - 1).abs()[fin].median()),
+        "median_abs_log_err_in_support_surrogate": float((sur.predict(q)[0] - exact)[:half].abs().median()),
+        "exact_underflow_queries": int((~fin).sum()),
+        "spread_tol": sur.spread_tol, "r2_max": sur.r2_max_,
+    }
+
+
+def run_surrogate(args) -> None:
+    import torch
+
+    import __graft_entry__ as ge
+
+    ge.build()
+    dev = torch.device("cuda", 0)
+    print(json.dumps({"surrogate": surrogate_workload(args, dev)}), flush=True)
+
+
 def run_op(args) -> None:
     """One operation alone (the profiling case for ncu captures): n GMM8
     points as data and as queries, Silverman bandwidth, W warm-up and K timed
@@ -441,6 +527,9 @@ def main():
     args = parse()
     if args.op:
         run_op(args)
+        return
+    if args.surrogate:
+        run_surrogate(args)
         return
     if args.impl == "reference":
         run_reference_arm(args)

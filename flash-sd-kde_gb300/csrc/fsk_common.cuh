@@ -40,7 +40,7 @@ enum KernelId {
   K_KDE1D = 5,
   K_KDE1D_SCORE = 6,
   K_SCORE16_TC = 7,
-  K_SCORE16_SYM_TC = 8,
+  K_MLP_INFER = 9,   // work unit: one (query, ensemble member) evaluation
 };
 
 // RAII bracket of one kernel launch with CUDA events on its stream when the
@@ -325,6 +325,11 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
 }
 
 // Store 16 consecutive 32-bit columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_st4(uint32_t taddr, const uint32_t (&r)[4]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(taddr), "r"(r[0]), "r"(r[1]),
+               "r"(r[2]), "r"(r[3]));
+}
+
 __device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16]) {
   asm volatile(
       "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "

@@ -1,0 +1,171 @@
+"""Learned surrogate of the exact 16-D KDE log-density (no counterpart in the
+reference; it serves bulk queries of a fitted Flash-SD-KDE model).
+
+    sur = SurrogateKDE(members=4).fit(debiased_data, h)
+    logp, served = sur.score_samples(queries, return_served=True)
+
+* Training pairs: queries = data points + N(0, (noise_scale h)^2 I), targets =
+  the exact normalised log-density from the tensor-core KDE kernel.
+* Model: an ensemble of MLPs 16 -> 256 -> 256 -> 256 -> 1 (SiLU, bf16
+  weights and activations, FP32 accumulation) on whitened inputs, fitted to
+  the residual of log p after a Gaussian base a + b r^2 (r the whitened
+  radius) that carries the tails; trained with the library's own forward,
+  backward and AdamW kernels (fsk_mlp_fwd / _bwd / _adam).
+* Serving: tensor-core inference of every member (fsk_mlp_infer), then the
+  gate: a query is served by the surrogate when the members agree
+  (max - min <= spread_tol, in log units) and its whitened radius is inside
+  the training distribution (r^2 <= the radius_quantile of the training
+  queries); every other query falls back to the exact KDE kernel, so the
+  exact path is also the judge of the surrogate's error.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from fsk import ops
+from globals import ND_FEATURES
+
+MLP_H = 256
+
+
+def _init_member(rng: np.random.Generator) -> np.ndarray:
+    """Weights uniform in +-sqrt(6/fan_in) (+-1/sqrt(256) for the output
+    vector), zero biases; the parameter layout of include/fsk.h."""
+    parts = []
+    for shape, bound in (((MLP_H, ND_FEATURES), math.sqrt(6.0 / ND_FEATURES)), ((MLP_H,), 0.0),
+                         ((MLP_H, MLP_H), math.sqrt(6.0 / MLP_H)), ((MLP_H,), 0.0),
+                         ((MLP_H, MLP_H), math.sqrt(6.0 / MLP_H)), ((MLP_H,), 0.0),
+                         ((MLP_H,), 1.0 / math.sqrt(MLP_H)), ((1,), 0.0)):
+        parts.append(rng.uniform(-bound, bound, size=shape).ravel() if bound > 0 else np.zeros(int(np.prod(shape))))
+    p = np.concatenate(parts).astype(np.float32)
+    assert p.size == ops.MLP_PARAMS
+    return p
+
+
+@dataclass
+class SurrogateKDE:
+    members: int = 4
+    epochs: int = 8
+    batch_size: int = 8192
+    lr: float = 2e-3
+    lr_final: float = 2e-5
+    weight_decay: float = 0.0
+    spread_tol: float = 0.03
+    radius_quantile: float = 0.999
+    noise_scale: float = 1.0
+    seed: int = 0
+    device: str | torch.device = "cuda"
+    history: list = field(default_factory=list)
+
+    # ---- exact targets ---------------------------------------------------------
+    def _exact_logp(self, queries: torch.Tensor, chunk: int = 1 << 20) -> torch.Tensor:
+        n = self.data_.shape[0]
+        h = self.bandwidth_
+        norm = 1.0 / ((2.0 * math.pi) ** (ND_FEATURES / 2.0) * h ** ND_FEATURES * n)
+        out = torch.empty(queries.shape[0], dtype=torch.float32, device=queries.device)
+        for s in range(0, queries.shape[0], chunk):
+            ops.kde16_sum(queries[s:s + chunk], self.data_, h, out_scale=norm, log_eps=0.0, out=out[s:s + chunk])
+        return out
+
+    def _radius2(self, x: torch.Tensor) -> torch.Tensor:
+        return (((x - self.in_mean_) * self.in_inv_std_) ** 2).sum(1)
+
+    # ---- fit -------------------------------------------------------------------
+    def fit(self, data, bandwidth: float, *, n_pairs: int = 4_000_000, queries=None, log_density=None,
+            verbose: bool = False) -> "SurrogateKDE":
+        if bandwidth <= 0:
+            raise ValueError("bandwidth must be positive.")
+        dev = ops._device(self.device)
+        self.data_ = ops.as_matrix(data, dev, ND_FEATURES)
+        if self.data_.shape[0] == 0:
+            raise ValueError("data must be non-empty.")
+        self.bandwidth_ = float(bandwidth)
+        g = torch.Generator(device=dev)
+        g.manual_seed(self.seed)
+        if queries is None:
+            idx = torch.randint(self.data_.shape[0], (n_pairs,), generator=g, device=dev)
+            noise = torch.randn((n_pairs, ND_FEATURES), generator=g, device=dev)
+            q = self.data_[idx] + noise * (self.noise_scale * self.bandwidth_)
+        else:
+            q = ops.as_matrix(queries, dev, ND_FEATURES)
+        logp = self._exact_logp(q) if log_density is None else ops.as_vector(log_density, dev)
+        ops.device_status(dev)
+        keep = torch.isfinite(logp)      # a query whose FP32 kernel sum underflows teaches nothing
+        if not bool(keep.all()):
+            q, logp = q[keep].contiguous(), logp[keep].contiguous()
+        if q.shape[0] == 0:
+            raise ValueError("no training query has a finite log-density.")
+        # whitening and the Gaussian base a + b r^2 (least squares)
+        self.in_mean_ = q.mean(0).contiguous()
+        self.in_inv_std_ = (1.0 / q.std(0).clamp_min(1e-12)).contiguous()
+        r2 = self._radius2(q)
+        A = torch.stack([torch.ones_like(r2), r2], 1).double()
+        coef = torch.linalg.lstsq(A, logp.double().unsqueeze(1)).solution.squeeze(1)
+        self.base_a_, self.base_b_ = float(coef[0]), float(coef[1])
+        resid = logp - (self.base_a_ + self.base_b_ * r2)
+        self.out_shift_ = float(resid.mean())
+        self.out_scale_ = float(resid.std().clamp_min(1e-12))
+        target = ((resid - self.out_shift_) / self.out_scale_).contiguous()
+        self.r2_max_ = float(torch.quantile(r2[: min(r2.numel(), 1 << 24)].float(), self.radius_quantile))
+        # parameters, optimiser state
+        rng = np.random.default_rng(self.seed)
+        params = torch.from_numpy(np.concatenate([_init_member(rng) for _ in range(self.members)])).to(dev)
+        m = torch.zeros_like(params)
+        v = torch.zeros_like(params)
+        grads = torch.empty_like(params)
+        B = min(self.batch_size, q.shape[0])
+        ws = ops.mlp_train_workspace(self.members, B, dev)
+        y = torch.empty((self.members, B), dtype=torch.float32, device=dev)
+        dy = torch.empty_like(y)
+        loss = torch.zeros(1, dtype=torch.float64, device=dev)
+        steps_per_epoch = q.shape[0] // B
+        total = max(1, self.epochs * steps_per_epoch)
+        step = 0
+        for epoch in range(self.epochs):
+            perm = torch.randperm(q.shape[0], generator=g, device=dev)
+            loss.zero_()
+            for s in range(steps_per_epoch):
+                sel = perm[s * B:(s + 1) * B]
+                xb = q[sel].contiguous()
+                tb = target[sel].contiguous()
+                ops.mlp_fwd(params, self.members, xb, self.in_mean_, self.in_inv_std_, ws, y)
+                ops.mlp_mse(y, tb, dy, loss)
+                ops.mlp_bwd(params, self.members, B, dy, ws, grads)
+                step += 1
+                lr = self.lr_final + 0.5 * (self.lr - self.lr_final) * (1.0 + math.cos(math.pi * step / total))
+                ops.mlp_adam(params, grads, m, v, step, lr, weight_decay=self.weight_decay)
+            ep_loss = float(loss.item()) / max(1, steps_per_epoch) / self.members
+            self.history.append(ep_loss)
+            if verbose:
+                print(f"epoch {epoch}: mse (normalised) {ep_loss:.3e}", flush=True)
+        ops.device_status(dev)
+        self.params_ = params
+        self.packed_ = ops.mlp_pack(params, self.members, self.in_mean_, self.in_inv_std_, self.out_scale_,
+                                    self.out_shift_)
+        return self
+
+    # ---- serving -----------------------------------------------------------------
+    def predict(self, queries) -> tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
+        """(log-density estimate, member spread, served mask) from the surrogate alone."""
+        dev = ops._device(self.device)
+        x = ops.as_matrix(queries, dev, ND_FEATURES)
+        y = ops.mlp_infer(self.packed_, self.members, x)
+        return ops.mlp_combine(y, x, self.in_mean_, self.in_inv_std_, self.base_a_, self.base_b_, self.spread_tol,
+                               self.r2_max_)
+
+    def score_samples(self, queries, *, return_served: bool = False):
+        """log-density of every query: surrogate where the gate serves it, the
+        exact KDE elsewhere."""
+        dev = ops._device(self.device)
+        x = ops.as_matrix(queries, dev, ND_FEATURES)
+        logp, _, served = self.predict(x)
+        miss = torch.nonzero(served == 0).squeeze(1)
+        if miss.numel():
+            logp[miss] = self._exact_logp(x[miss].contiguous())
+        if return_served:
+            return logp, served.bool()
+        return logp

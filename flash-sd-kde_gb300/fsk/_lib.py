@@ -32,6 +32,10 @@ FSK_WEIGHTED_FEATURE_MAJOR = 0x10
 FSK_SCORE_ORDERED = 0
 FSK_SCORE_SYMMETRIC = 1
 
+FSK_MLP_IN = 16
+FSK_MLP_HIDDEN = 256
+FSK_MLP_PARAMS = 136193
+
 FSK_RULE_SILVERMAN = 0
 FSK_RULE_SDKDE_1D = 1
 
@@ -56,6 +60,17 @@ SIGNATURES: dict[str, tuple] = {
     "fsk_silverman_workspace_bytes": (_sz, [_i64, _int]),
     "fsk_silverman": (_int, [_vp, _i64, _int, _int, _vp, _vp, _sz, _vp]),
     "fsk_reduce_partials": (_int, [_vp, _i64, _i64, _vp, _vp]),
+    "fsk_mlp_train_workspace_bytes": (_sz, [_int, _i64]),
+    "fsk_mlp_fwd": (_int, [_vp, _int, _vp, _i64, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "fsk_mlp_bwd": (_int, [_vp, _int, _i64, _vp, _vp, _vp, _sz, _vp]),
+    "fsk_mlp_mse": (_int, [_vp, _vp, _i64, _int, _vp, _vp, _vp]),
+    "fsk_mlp_adam": (_int, [_vp, _vp, _vp, _vp, _i64, _c.c_float, _c.c_float, _c.c_float, _c.c_float,
+                            _c.c_float, _int, _vp]),
+    "fsk_mlp_packed_bytes": (_sz, [_int]),
+    "fsk_mlp_pack": (_int, [_vp, _int, _vp, _vp, _c.c_float, _c.c_float, _vp, _vp]),
+    "fsk_mlp_infer": (_int, [_vp, _int, _vp, _i64, _vp, _vp]),
+    "fsk_mlp_combine": (_int, [_vp, _int, _i64, _vp, _vp, _vp, _c.c_float, _c.c_float, _c.c_float, _c.c_float,
+                               _vp, _vp, _vp, _vp]),
     "fsk_device_status": (_int, [_vp]),
     "fsk_strerror": (_c.c_char_p, [_int]),
     "fsk_version": (_int, []),

@@ -272,3 +272,100 @@ def mma_ts_probe(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
         st = L.load().fsk_diag_mma_ts_probe(a.data_ptr(), b.data_ptr(), d.data_ptr(), _stream(dev))
     L.check(st, "fsk_diag_mma_ts_probe")
     return d
+
+
+# ---- learned surrogate (include/fsk.h, "learned surrogate") ----------------------
+MLP_PARAMS = L.FSK_MLP_PARAMS
+
+
+def _mlp_check(params: torch.Tensor, members: int) -> None:
+    if params.dtype != torch.float32 or not params.is_contiguous() or params.numel() != members * MLP_PARAMS:
+        raise ValueError(f"params must be a contiguous float32 tensor of {members} x {MLP_PARAMS} values")
+
+
+def mlp_train_workspace(members: int, batch: int, device) -> torch.Tensor:
+    return _workspace(L.load().fsk_mlp_train_workspace_bytes(members, batch), _device(device))
+
+
+def mlp_fwd(params, members, x, in_mean, in_inv_std, ws, y=None) -> torch.Tensor:
+    """Training forward; keeps the activations in `ws` for mlp_bwd. y: (members, batch)."""
+    _mlp_check(params, members)
+    dev = _device(params.device)
+    batch = x.shape[0]
+    if y is None:
+        y = torch.empty((members, batch), dtype=torch.float32, device=dev)
+    with torch.cuda.device(dev):
+        st = L.load().fsk_mlp_fwd(params.data_ptr(), members, x.data_ptr(), batch, in_mean.data_ptr(),
+                                  in_inv_std.data_ptr(), y.data_ptr(), ws.data_ptr(), ws.numel(), _stream(dev))
+    L.check(st, "fsk_mlp_fwd")
+    return y
+
+
+def mlp_bwd(params, members, batch, dy, ws, grads=None) -> torch.Tensor:
+    _mlp_check(params, members)
+    dev = _device(params.device)
+    if grads is None:
+        grads = torch.empty_like(params)
+    with torch.cuda.device(dev):
+        st = L.load().fsk_mlp_bwd(params.data_ptr(), members, batch, dy.data_ptr(), grads.data_ptr(),
+                                  ws.data_ptr(), ws.numel(), _stream(dev))
+    L.check(st, "fsk_mlp_bwd")
+    return grads
+
+
+def mlp_mse(y, target, dy, loss=None) -> None:
+    members, batch = y.shape
+    dev = _device(y.device)
+    with torch.cuda.device(dev):
+        st = L.load().fsk_mlp_mse(y.data_ptr(), target.data_ptr(), batch, members, dy.data_ptr(),
+                                  _ptr(loss), _stream(dev))
+    L.check(st, "fsk_mlp_mse")
+
+
+def mlp_adam(params, grads, m, v, step, lr, beta1=0.9, beta2=0.999, eps=1e-8, weight_decay=0.0) -> None:
+    dev = _device(params.device)
+    with torch.cuda.device(dev):
+        st = L.load().fsk_mlp_adam(params.data_ptr(), grads.data_ptr(), m.data_ptr(), v.data_ptr(),
+                                   params.numel(), float(lr), float(beta1), float(beta2), float(eps),
+                                   float(weight_decay), int(step), _stream(dev))
+    L.check(st, "fsk_mlp_adam")
+
+
+def mlp_pack(params, members, in_mean, in_inv_std, out_scale=1.0, out_shift=0.0) -> torch.Tensor:
+    _mlp_check(params, members)
+    dev = _device(params.device)
+    lib = L.load()
+    packed = torch.empty(lib.fsk_mlp_packed_bytes(members), dtype=torch.uint8, device=dev)
+    with torch.cuda.device(dev):
+        st = lib.fsk_mlp_pack(params.data_ptr(), members, in_mean.data_ptr(), in_inv_std.data_ptr(),
+                              float(out_scale), float(out_shift), packed.data_ptr(), _stream(dev))
+    L.check(st, "fsk_mlp_pack")
+    return packed
+
+
+def mlp_infer(packed, members, x, y=None) -> torch.Tensor:
+    """Tensor-core inference of every member: (members, batch)."""
+    dev = _device(packed.device)
+    batch = x.shape[0]
+    if y is None:
+        y = torch.empty((members, batch), dtype=torch.float32, device=dev)
+    with torch.cuda.device(dev):
+        st = L.load().fsk_mlp_infer(packed.data_ptr(), members, x.data_ptr(), batch, y.data_ptr(), _stream(dev))
+    L.check(st, "fsk_mlp_infer")
+    return y
+
+
+def mlp_combine(y, x=None, in_mean=None, in_inv_std=None, base_a=0.0, base_b=0.0, spread_tol=float("inf"),
+                r2_max=float("inf")):
+    """(mean + base, spread, served mask) over the members of y (members, batch)."""
+    members, batch = y.shape
+    dev = _device(y.device)
+    mean = torch.empty(batch, dtype=torch.float32, device=dev)
+    spread = torch.empty(batch, dtype=torch.float32, device=dev)
+    served = torch.empty(batch, dtype=torch.uint8, device=dev)
+    with torch.cuda.device(dev):
+        st = L.load().fsk_mlp_combine(y.data_ptr(), members, batch, _ptr(x), _ptr(in_mean), _ptr(in_inv_std),
+                                      float(base_a), float(base_b), float(spread_tol), float(r2_max),
+                                      mean.data_ptr(), spread.data_ptr(), served.data_ptr(), _stream(dev))
+    L.check(st, "fsk_mlp_combine")
+    return mean, spread, served

@@ -158,6 +158,50 @@ FSK_API int fsk_silverman(const float* data, int64_t n, int d, int rule, double*
 FSK_API int fsk_reduce_partials(const float* partials, int64_t splits, int64_t count,
                                 float* out, void* stream);
 
+/* ---- learned surrogate (no counterpart in the reference) ------------------ */
+/* An ensemble of `members` (1..8) MLPs 16 -> 256 -> 256 -> 256 -> 1 with SiLU,
+ * bf16 weights and activations, FP32 accumulation:
+ *   a0 = bf16((x - in_mean) * in_inv_std)
+ *   a_l = bf16(silu(bf16(W_l) a_{l-1} + b_l)), l = 1..3;  y = bf16(w4) . a3 + b4
+ * FP32 parameters of a member, contiguous (FSK_MLP_PARAMS floats):
+ *   W1[256][16] b1[256] W2[256][256] b2[256] W3[256][256] b3[256] w4[256] b4
+ * Members are stored back to back.  in_mean / in_inv_std are 16-float device
+ * arrays.  Training: fsk_mlp_fwd keeps the activations in the workspace for
+ * fsk_mlp_bwd (same members, batch and workspace), which overwrites `grads`
+ * with d(sum dy*y)/d(params), straight-through for the bf16 roundings. */
+#define FSK_MLP_IN 16
+#define FSK_MLP_HIDDEN 256
+#define FSK_MLP_PARAMS 136193
+FSK_API size_t fsk_mlp_train_workspace_bytes(int members, int64_t batch);
+FSK_API int fsk_mlp_fwd(const float* params, int members, const float* x, int64_t batch,
+                        const float* in_mean, const float* in_inv_std, float* y /* [members][batch] */,
+                        void* workspace, size_t workspace_bytes, void* stream);
+FSK_API int fsk_mlp_bwd(const float* params, int members, int64_t batch, const float* dy /* [members][batch] */,
+                        float* grads, void* workspace, size_t workspace_bytes, void* stream);
+/* dy = 2 (y - target) / batch per member; *loss (device FP64, may be NULL) +=
+ * sum over members of mean squared error. */
+FSK_API int fsk_mlp_mse(const float* y, const float* target, int64_t batch, int members, float* dy,
+                        double* loss, void* stream);
+/* AdamW step `step` (from 1) over `count` parameters, bias-corrected. */
+FSK_API int fsk_mlp_adam(float* params, const float* grads, float* m, float* v, int64_t count, float lr,
+                         float beta1, float beta2, float eps, float weight_decay, int step, void* stream);
+/* Inference image (bf16 weights in the tensor-core kernel's layouts, the input
+ * normalisation and an output affine y' = y * out_scale + out_shift). */
+FSK_API size_t fsk_mlp_packed_bytes(int members);
+FSK_API int fsk_mlp_pack(const float* params, int members, const float* in_mean, const float* in_inv_std,
+                         float out_scale, float out_shift, void* packed, void* stream);
+/* Tensor-core inference: y[member][b] for all members (x 16-byte aligned). */
+FSK_API int fsk_mlp_infer(const void* packed, int members, const float* x, int64_t batch, float* y,
+                          void* stream);
+/* Ensemble statistics and serving gate per query b (outputs may be NULL):
+ *   r2 = |(x_b - in_mean) * in_inv_std|^2 when x is given, else 0
+ *   mean[b] = average_m y[m][b] + base_a + base_b * r2
+ *   spread[b] = max_m y[m][b] - min_m y[m][b]
+ *   served[b] = spread <= spread_tol && r2 <= r2_max */
+FSK_API int fsk_mlp_combine(const float* y, int members, int64_t batch, const float* x, const float* in_mean,
+                            const float* in_inv_std, float base_a, float base_b, float spread_tol, float r2_max,
+                            float* mean, float* spread, uint8_t* served, void* stream);
+
 /* ---- diagnostics --------------------------------------------------------- */
 /* Synchronises the stream, reads and clears the library's device error word.
  * Returns FSK_OK, FSK_ERR_DEVICE_TIMEOUT or FSK_ERR_CUDA. */
@@ -193,7 +237,7 @@ FSK_API int fsk_diag_pipe_rates(double* rates_out, void* stream);
 /* ---- measurement hooks (no counterpart in the reference) ------------------ */
 /* Kernel ids: 1 tensor-core 16-D KDE, 2 CUDA-core 16-D KDE, 3 CUDA-core
  * ordered score, 4 CUDA-core symmetric score, 5 1-D KDE, 6 1-D KDE score,
- * 7 tensor-core score. */
+ * 7 tensor-core score, 9 surrogate inference (unit: one query x member). */
 /* When enabled, each hot-path kernel launch is bracketed by CUDA events on
  * its own stream. */
 FSK_API void fsk_timer_enable(int on);

@@ -66,6 +66,13 @@ def test_argument_validation_is_host_side(lib):
     assert lib.fsk_silverman(fake, 10, 2, 1, fake, fake, 1 << 20, None) == inval
     assert lib.fsk_kde1d(fake, 10, fake, 0, 1.0, 0, 1.0, 0.0, fake, fake, 1 << 20, None) == inval
     assert lib.fsk_reduce_partials(fake, 0, 10, fake, None) == inval
+    assert lib.fsk_mlp_fwd(fake, 0, fake, 10, fake, fake, fake, fake, 1 << 20, None) == inval
+    assert lib.fsk_mlp_fwd(fake, 9, fake, 10, fake, fake, fake, fake, 1 << 20, None) == inval
+    assert lib.fsk_mlp_bwd(fake, 2, 0, fake, fake, fake, 1 << 20, None) == inval
+    assert lib.fsk_mlp_adam(fake, fake, fake, fake, 10, 1e-3, 1.0, 0.999, 1e-8, 0.0, 1, None) == inval
+    assert lib.fsk_mlp_adam(fake, fake, fake, fake, 10, 1e-3, 0.9, 0.999, 1e-8, 0.0, 0, None) == inval
+    assert lib.fsk_mlp_infer(fake, 4, 17, 10, fake, None) == inval        # misaligned x
+    assert lib.fsk_mlp_combine(fake, 4, 10, fake, None, None, 0.0, 0.0, 1.0, 1.0, None, None, None, None) == inval
 
 
 def test_workspace_sizes(lib):
@@ -73,5 +80,8 @@ def test_workspace_sizes(lib):
     b = lib.fsk_kde16_workspace_bytes(1 << 20, 1 << 20, 0)
     assert 0 < a < b
     assert lib.fsk_kde16_workspace_bytes(0, 10, 0) == 0
+    assert lib.fsk_mlp_train_workspace_bytes(4, 8192) >= 4 * 8192 * 256 * 4 * 7
+    assert lib.fsk_mlp_train_workspace_bytes(0, 8192) == 0
+    assert lib.fsk_mlp_packed_bytes(4) == 4 * (256 + 4096 + 8192 + 2 * 16 * 8192)
     assert lib.fsk_empscore16_workspace_bytes(1 << 16, 0, 0) > (1 << 16) * 17 * 8
     assert lib.fsk_silverman_workspace_bytes(100, 16) > 0

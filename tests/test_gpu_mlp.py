@@ -1,0 +1,156 @@
+"""Learned surrogate kernels on the GPU against the oracle (oracle/mlp.py) and
+against each other, plus the estimator's gate and exact fallback.
+
+Tolerances: the kernels compute SiLU through tanh.approx (max relative error
+~2^-11) while the oracle uses the exact sigmoid; with bf16 activations this
+flips an occasional bf16 rounding, so forward values are compared at
+1e-2 * (1 + |y|) and gradients at 3e-2 relative L2 norm.  Adam is FP32 vs
+FP64 (1e-5 relative).  The tensor-core inference and the CUDA-core training
+forward compute the same model in a different accumulation order:
+1e-2 * (1 + |y|).
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import mlp as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(seed, batch, members):
+    rng = np.random.default_rng(seed)
+    params = np.concatenate([O.init_params(rng) for _ in range(members)])
+    x = (rng.standard_normal((batch, 16)) * 3.0 + 1.0).astype(np.float32)
+    mean = (rng.standard_normal(16) * 0.5).astype(np.float32)
+    istd = rng.uniform(0.3, 0.6, 16).astype(np.float32)
+    return rng, params, x, mean, istd
+
+
+def _dev(a, dev):
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+@pytest.mark.parametrize("batch,members", [(200, 1), (1000, 4), (64, 2)])
+def test_training_forward_matches_oracle(cuda_dev, batch, members):
+    from fsk import ops
+
+    _, params, x, mean, istd = _case(0, batch, members)
+    P, X, M, S = (_dev(a, cuda_dev) for a in (params, x, mean, istd))
+    ws = ops.mlp_train_workspace(members, batch, cuda_dev)
+    y = ops.mlp_fwd(P, members, X, M, S, ws).cpu().numpy()
+    for k in range(members):
+        ref, _ = O.forward(params[k * O.N_PARAMS:(k + 1) * O.N_PARAMS], x, mean, istd, quantize=True)
+        assert np.all(np.abs(y[k] - ref) <= 1e-2 * (1 + np.abs(ref))), np.abs(y[k] - ref).max()
+
+
+def test_backward_matches_oracle(cuda_dev):
+    from fsk import ops
+
+    batch, members = 777, 2
+    rng, params, x, mean, istd = _case(1, batch, members)
+    dy = rng.standard_normal((members, batch)).astype(np.float32) / batch
+    P, X, M, S, DY = (_dev(a, cuda_dev) for a in (params, x, mean, istd, dy))
+    ws = ops.mlp_train_workspace(members, batch, cuda_dev)
+    ops.mlp_fwd(P, members, X, M, S, ws)
+    g = ops.mlp_bwd(P, members, batch, DY, ws).cpu().numpy()
+    for k in range(members):
+        pk = params[k * O.N_PARAMS:(k + 1) * O.N_PARAMS]
+        _, cache = O.forward(pk, x, mean, istd, quantize=True)
+        ref = O.backward(cache, dy[k].astype(np.float64))
+        got = g[k * O.N_PARAMS:(k + 1) * O.N_PARAMS]
+        for name, lo, hi in (("W1", 0, 4096), ("W2", 4352, 4352 + 65536), ("W3", 70144, 70144 + 65536),
+                             ("w4", 135936, 136192), ("all", 0, O.N_PARAMS)):
+            r = np.linalg.norm(got[lo:hi] - ref[lo:hi]) / np.linalg.norm(ref[lo:hi])
+            assert r < 3e-2, (k, name, r)
+
+
+def test_adam_matches_oracle(cuda_dev):
+    from fsk import ops
+
+    rng = np.random.default_rng(2)
+    n = 5000
+    p, g = rng.standard_normal(n).astype(np.float32), rng.standard_normal(n).astype(np.float32)
+    m, v = (rng.standard_normal(n) * 0.1).astype(np.float32), rng.uniform(0, 0.1, n).astype(np.float32)
+    P, G, Mt, Vt = (_dev(a, cuda_dev) for a in (p, g, m, v))
+    ops.mlp_adam(P, G, Mt, Vt, step=7, lr=3e-3, weight_decay=0.01)
+    # the kernel holds beta1, beta2 in FP32: give the oracle the same constants
+    b1, b2 = float(np.float32(0.9)), float(np.float32(0.999))
+    rp, rm, rv = O.adam(p, g, m, v, step=7, lr=3e-3, beta1=b1, beta2=b2, weight_decay=0.01)
+    np.testing.assert_allclose(P.cpu().numpy(), rp, rtol=1e-5, atol=1e-7)
+    np.testing.assert_allclose(Mt.cpu().numpy(), rm, rtol=1e-5, atol=1e-7)
+    np.testing.assert_allclose(Vt.cpu().numpy(), rv, rtol=1e-5, atol=1e-9)
+
+
+@pytest.mark.parametrize("batch", [1, 127, 129, 1000, 5000])
+def test_tensor_core_inference_matches_training_forward(cuda_dev, batch):
+    from fsk import ops
+
+    members = 4
+    _, params, x, mean, istd = _case(3, batch, members)
+    P, X, M, S = (_dev(a, cuda_dev) for a in (params, x, mean, istd))
+    ws = ops.mlp_train_workspace(members, batch, cuda_dev)
+    y_train = ops.mlp_fwd(P, members, X, M, S, ws)
+    packed = ops.mlp_pack(P, members, M, S, out_scale=2.0, out_shift=-1.5)
+    y_inf = ops.mlp_infer(packed, members, X)
+    ops.device_status(cuda_dev)
+    a, b = y_inf.cpu().numpy(), (y_train * 2.0 - 1.5).cpu().numpy()
+    assert np.all(np.isfinite(a))
+    assert np.all(np.abs(a - b) <= 1e-2 * (1 + np.abs(b))), np.abs(a - b).max()
+
+
+def test_combine_gate(cuda_dev):
+    from fsk import ops
+
+    rng = np.random.default_rng(4)
+    members, batch = 3, 1000
+    y = rng.standard_normal((members, batch)).astype(np.float32) * 0.02
+    x = rng.standard_normal((batch, 16)).astype(np.float32) * 2
+    mean = rng.standard_normal(16).astype(np.float32) * 0.1
+    istd = rng.uniform(0.5, 1.0, 16).astype(np.float32)
+    Y, X, M, S = (_dev(a, cuda_dev) for a in (y, x, mean, istd))
+    mu, sp, served = ops.mlp_combine(Y, X, M, S, base_a=-3.0, base_b=-0.25, spread_tol=0.05, r2_max=20.0)
+    r2 = (((x - mean) * istd) ** 2).sum(1)
+    np.testing.assert_allclose(mu.cpu().numpy(), y.mean(0) - 3.0 - 0.25 * r2, rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(sp.cpu().numpy(), y.max(0) - y.min(0), rtol=1e-6, atol=1e-7)
+    want = (y.max(0) - y.min(0) <= 0.05) & (r2 <= 20.0)
+    got = served.cpu().numpy().astype(bool)
+    # ties at the threshold may round either way
+    assert np.mean(got == want) > 0.999 and want.any() and (~want).any()
+
+
+def test_surrogate_fit_gate_and_exact_fallback(cuda_dev):
+    """A small end-to-end fit: the surrogate serves in-support queries within a
+    few percent and every query it does not serve equals the exact KDE."""
+    from flash_sd_kde.surrogate import SurrogateKDE
+    from fsk import ops, workloads
+
+    x_np, _ = workloads.gmm8_16d(4096, 16)
+    x = torch.from_numpy(x_np).to(cuda_dev)
+    h = float(ops.silverman(x).item())
+    sur = SurrogateKDE(members=4, epochs=4, batch_size=4096, spread_tol=0.05, seed=1).fit(x, h, n_pairs=200_000)
+    assert len(sur.history) == 4 and sur.history[-1] < sur.history[0]
+    g = torch.Generator(device=cuda_dev).manual_seed(9)
+    idx = torch.randint(4096, (20000,), generator=g, device=cuda_dev)
+    q_in = x[idx] + torch.randn((20000, 16), generator=g, device=cuda_dev) * h
+    q_out = torch.randn((5000, 16), generator=g, device=cuda_dev) * 3.0
+    q = torch.cat([q_in, q_out]).contiguous()
+    logp, served = sur.score_samples(q, return_served=True)
+    exact = sur._exact_logp(q)
+    ops.device_status(cuda_dev)
+    miss = ~served
+    assert miss.any() and served.any()
+    # fallback queries are the exact kernel's values for that query set, bit
+    # for bit (the tensor-core KDE's operand scaling depends on the query
+    # set, so against the whole set they agree to ~1e-6, not bitwise)
+    assert torch.equal(logp[miss], sur._exact_logp(q[miss].contiguous()))
+    # far queries may underflow the FP32 kernel sum to log 0 = -inf on both sides
+    fin = torch.isfinite(exact) & miss
+    assert torch.equal(torch.isinf(logp[miss]), torch.isinf(exact[miss]))
+    assert float((logp[fin] - exact[fin]).abs().max()) < 1e-4
+    rel = (torch.exp((logp - exact).double()) - 1).abs()
+    # every served query has a finite exact value to compare with here
+    assert bool(torch.isfinite(exact[served]).all())
+    assert float(rel[served].median()) < 0.1, float(rel[served].median())
