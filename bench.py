@@ -20,6 +20,9 @@ roofline   the dominant kernel's pair-evals/s (library timer: CUDA events on
            ex2 and FP32 FMA rates measured on this GPU.
 cpu_baseline  the reference CPU path (numpy restatement) on a bounded
            sample with all host cores, in a subprocess.
+surrogate  the learned-surrogate workload (exact SD-KDE fit on 262144 points,
+           4 MLPs trained on 4M pairs, 1M held-out queries): gated,
+           surrogate-only and exact queries/s, served fraction, errors.
 Multi-GPU (torchrun): every rank runs an independent replica (own query
 set, shared training set); value = all ranks' pairs / max-over-ranks time.
 """
@@ -361,6 +364,13 @@ def run_gpu_arm(args) -> None:
     deb64 = xs[:64] + 0.5 * ((phi @ xs) / (phi.sum(1, keepdims=True) + EPS) - xs[:64])
     deb_abs = float(np.abs(deb_np[:64] - deb64).max())
 
+    surrogate = None
+    if rank == 0 and not args.no_surrogate:
+        try:
+            surrogate = surrogate_workload(args, dev)
+        except Exception as exc:  # reported, not fatal
+            surrogate = {"error": str(exc)[-300:]}
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
@@ -399,6 +409,7 @@ def run_gpu_arm(args) -> None:
             "roofline_tensor": tensor_roofline(dom, achieved),
             "kernels": kernels,
             "cpu_baseline": cpu,
+            "surrogate": surrogate,
             "clocks": sampler.summary(),
             "accuracy": {"kde_max_rel_vs_fp64": float(kde_rel.max()), "kde_queries_checked": 128,
                          "debias_max_abs_vs_fp64": deb_abs, "debias_rows_checked": 64},

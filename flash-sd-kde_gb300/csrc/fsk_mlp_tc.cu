@@ -8,7 +8,7 @@
 //   A1 = bf16(silu(D + b1))                  TMEM -> registers -> TMEM cols 256..383
 //   D  = A1 . W2^T                           16 MMAs (K steps), N=256
 //   A2 = bf16(silu(D + b2)); D = A2 . W3^T   16 MMAs
-//   y  = bf16(silu(D + b3)) . bf16(w4) + b4  per-thread dot, two column halves combined
+//   y  = bf16(silu(D + b3)) . bf16(w4) + b4  per-thread dot, four feature quarters combined
 // The activations stay in tensor memory as the A operand of the next layer
 // (tcgen05.mma with A in TMEM), so nothing is transposed through shared
 // memory.  W2 and W3 (128 KB each in bf16) do not fit in shared memory next
@@ -16,8 +16,8 @@
 // core-matrix K-major) through a ring of RING slots; W1, the biases, w4 and
 // the input normalisation are loaded once per CTA.
 //
-// Warps: 0-7 epilogue (warp w: TMEM lane quarter w&3, feature half w>>2),
-// 8 producer (bulk copies), 9 MMA issue + TMEM owner.
+// Warps: 0-15 epilogue (warp w: TMEM lane quarter w&3, feature quarter
+// w>>2), 16 producer (bulk copies), 17 MMA issue + TMEM owner.
 #include <cuda_bf16.h>
 
 #include "fsk_kernels.cuh"
@@ -33,7 +33,7 @@ namespace {
 constexpr int QT = 128;                         // queries per tile
 constexpr int SLICE_BYTES = MLP_H * 16 * 2;     // one K slice: [256][16] bf16 = 8 KB
 constexpr int N_SLICES = MLP_H / 16;            // 16 per hidden layer
-constexpr int RING = 8;
+constexpr int RING = 24;                        // slices in flight: hides L2 latency across layers
 // packed member image (global):
 //   header 256 B: in_mean[16] in_inv_std[16] out_scale out_shift b4 (FP32)
 //   b1 b2 b3 w4 (FP32, w4 bf16-rounded) 4 KB
@@ -48,12 +48,13 @@ constexpr int MEMBER_BYTES = W3_OFF + N_SLICES * SLICE_BYTES;
 constexpr int SM_CONST_BYTES = W2_OFF;                     // header + vectors + W1 image (one copy)
 constexpr int SM_RING_OFF = SM_CONST_BYTES;
 constexpr int SM_YSUM_OFF = SM_RING_OFF + RING * SLICE_BYTES;
-constexpr int SM_BAR_OFF = SM_YSUM_OFF + QT * 4;
-constexpr int SMEM_BYTES = SM_BAR_OFF + 256;
-constexpr int EPI_WARPS = 8;
-constexpr int PROD_WARP = 8;
-constexpr int MMA_WARP = 9;
-constexpr int THREADS = 10 * 32;
+constexpr int SM_BAR_OFF = SM_YSUM_OFF + 3 * QT * 4;
+constexpr int N_BARS = 5 + 2 * RING;             // cready, full/empty ring, aready, dfull, ycomb, drain
+constexpr int SMEM_BYTES = SM_BAR_OFF + (N_BARS + 1) * 8;   // + the TMEM address slot
+constexpr int EPI_WARPS = 16;
+constexpr int PROD_WARP = 16;
+constexpr int MMA_WARP = 17;
+constexpr int THREADS = 18 * 32;
 constexpr int T_D = 0;       // accumulator: 256 FP32 columns
 constexpr int T_A = 256;     // activations: 128 columns of packed bf16 pairs
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
@@ -95,9 +96,9 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_infer_kernel(InferParams p) {
   uint64_t* cready = bars;               // constants loaded
   uint64_t* full = bars + 1;             // [RING]
   uint64_t* empty = bars + 1 + RING;     // [RING]
-  uint64_t* aready = bars + 1 + 2 * RING;  // activations (or inputs) stored, 8 warps
+  uint64_t* aready = bars + 1 + 2 * RING;  // activations (or inputs) stored, all epilogue warps
   uint64_t* dfull = bars + 2 + 2 * RING;   // layer accumulator complete
-  uint64_t* ycomb = bars + 3 + 2 * RING;   // feature-half-1 partial dots stored, 4 warps
+  uint64_t* ycomb = bars + 3 + 2 * RING;   // partial dots of feature quarters 1-3 stored, 12 warps
   uint64_t* drain = bars + 4 + 2 * RING;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 5 + 2 * RING);
   int64_t n_ring_copies = 0;
@@ -116,7 +117,7 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_infer_kernel(InferParams p) {
     }
     mbar_init(aready, EPI_WARPS);
     mbar_init(dfull, 1);
-    mbar_init(ycomb, 4);
+    mbar_init(ycomb, 12);
     mbar_init(drain, 1);
     fence_barrier_init();
   }
@@ -177,8 +178,8 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_infer_kernel(InferParams p) {
       }
     }
   } else {
-    // ---------------- epilogue: thread = one query, one feature half ----------------
-    const int quarter = warp & 3, half = warp >> 2;
+    // ---------------- epilogue: thread = one query, one feature quarter ----------------
+    const int quarter = warp & 3, fq = warp >> 2;   // TMEM lane quarter, feature quarter (64 features)
     const int row = quarter * 32 + lane;
     const uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
     if (!mbar_wait(cready, 0, 56)) goto done;
@@ -186,26 +187,24 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_infer_kernel(InferParams p) {
     const float* inv_std = hdr + 16;
     const float out_scale = hdr[32], out_shift = hdr[33], b4 = hdr[34];
     int k = 0;
+    // this thread's 4 input features of a tile (features 4 fq .. 4 fq + 3);
+    // the next tile's are loaded while the current one runs
+    auto load_x = [&](int64_t tile) {
+      const int64_t qq = tile * QT + row;
+      if (tile < p.tiles && qq < p.batch) return __ldg(reinterpret_cast<const float4*>(p.x + qq * MLP_IN + 4 * fq));
+      return make_float4(mean[4 * fq], mean[4 * fq + 1], mean[4 * fq + 2], mean[4 * fq + 3]);
+    };
+    float4 xv = load_x(group);
     for (int64_t t = group; t < p.tiles; t += groups) {
       const int64_t q = t * QT + row;
-      // inputs: half h stores features 8h..8h+7 (4 packed columns)
       {
-        float v[8];
-        if (q < p.batch) {
-          const float4* xr = reinterpret_cast<const float4*>(p.x + q * MLP_IN + 8 * half);
-          const float4 a = __ldg(xr), b = __ldg(xr + 1);
-          v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-        } else {
-#pragma unroll
-          for (int j = 0; j < 8; ++j) v[j] = mean[8 * half + j];
-        }
-        uint32_t pk[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int f = 8 * half + 2 * j;
-          pk[j] = pack_bf16((v[2 * j] - mean[f]) * inv_std[f], (v[2 * j + 1] - mean[f + 1]) * inv_std[f + 1]);
-        }
-        tmem_st4(tmem + lane_off + T_A + 4 * half, pk);
+        const float4 v = xv;
+        xv = load_x(t + groups);
+        const int f = 4 * fq;
+        uint32_t pk[2];
+        pk[0] = pack_bf16((v.x - mean[f]) * inv_std[f], (v.y - mean[f + 1]) * inv_std[f + 1]);
+        pk[1] = pack_bf16((v.z - mean[f + 2]) * inv_std[f + 2], (v.w - mean[f + 3]) * inv_std[f + 3]);
+        tmem_st2(tmem + lane_off + T_A + 2 * fq, pk);
         tmem_st_wait();
         tc_fence_before();
         __syncwarp();
@@ -216,22 +215,21 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_infer_kernel(InferParams p) {
         if (!mbar_wait(dfull, (uint32_t)(k & 1), 57)) goto done;
         tc_fence_after();
         ++k;
-        const float* bias = vec + layer * MLP_H + 128 * half;
-        const float* w4 = vec + 3 * MLP_H + 128 * half;
+        const float* bias = vec + layer * MLP_H + 64 * fq;
+        const float* w4 = vec + 3 * MLP_H + 64 * fq;
 #pragma unroll 1
-        for (int c = 0; c < 4; ++c) {
+        for (int c = 0; c < 2; ++c) {
           uint32_t r[32];
-          tmem_ld32(tmem + lane_off + T_D + 128 * half + 32 * c, r);
+          tmem_ld32(tmem + lane_off + T_D + 64 * fq + 32 * c, r);
           tmem_ld_wait();
           if (layer < 2) {
             uint32_t pk[16];
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
-              const float z0 = __uint_as_float(r[2 * j]) + bias[32 * c + 2 * j];
-              const float z1 = __uint_as_float(r[2 * j + 1]) + bias[32 * c + 2 * j + 1];
-              pk[j] = pack_bf16(silu_fast(z0), silu_fast(z1));
+              const float2 bb = *reinterpret_cast<const float2*>(bias + 32 * c + 2 * j);
+              pk[j] = pack_bf16(silu_fast(__uint_as_float(r[2 * j]) + bb.x), silu_fast(__uint_as_float(r[2 * j + 1]) + bb.y));
             }
-            tmem_st16(tmem + lane_off + T_A + 64 * half + 16 * c, pk);
+            tmem_st16(tmem + lane_off + T_A + 32 * fq + 16 * c, pk);
           } else {
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
@@ -247,16 +245,16 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_infer_kernel(InferParams p) {
           if (lane == 0) mbar_arrive(aready);
         }
       }
-      // combine the two feature halves of each query's dot product
+      // combine the four feature quarters of each query's dot product
       tc_fence_before();
-      if (half == 1) {
-        ysum[row] = acc_y;
+      if (fq != 0) {
+        ysum[(fq - 1) * QT + row] = acc_y;
         __syncwarp();
         if (lane == 0) mbar_arrive(ycomb);
       } else {
         const int kt = (int)((t - group) / groups);
         if (!mbar_wait(ycomb, (uint32_t)(kt & 1), 58)) goto done;
-        const float v = acc_y + ysum[row] + b4;
+        const float v = acc_y + ysum[row] + ysum[QT + row] + ysum[2 * QT + row] + b4;
         if (q < p.batch) p.y[(int64_t)member * p.batch + q] = fmaf(v, out_scale, out_shift);
       }
     }

@@ -103,9 +103,11 @@ class SurrogateKDE:
         self.in_mean_ = q.mean(0).contiguous()
         self.in_inv_std_ = (1.0 / q.std(0).clamp_min(1e-12)).contiguous()
         r2 = self._radius2(q)
-        A = torch.stack([torch.ones_like(r2), r2], 1).double()
-        coef = torch.linalg.lstsq(A, logp.double().unsqueeze(1)).solution.squeeze(1)
-        self.base_a_, self.base_b_ = float(coef[0]), float(coef[1])
+        r2d, lpd = r2.double(), logp.double()
+        rm, lm = r2d.mean(), lpd.mean()
+        var = ((r2d - rm) ** 2).mean()
+        b = ((r2d - rm) * (lpd - lm)).mean() / var if float(var) > 0 else torch.zeros((), dtype=torch.float64)
+        self.base_a_, self.base_b_ = float(lm - b * rm), float(b)
         resid = logp - (self.base_a_ + self.base_b_ * r2)
         self.out_shift_ = float(resid.mean())
         self.out_scale_ = float(resid.std().clamp_min(1e-12))
