@@ -14,24 +14,38 @@ constexpr int KH = 32;                  // K of the "hi" operand: 16 features + 
 // Operand images, fp16, no-swizzle K-major core-matrix layout: 8-row groups,
 // each group = (K/8) core matrices of 8 rows x 16 B stored back to back.
 constexpr int H_ROW_BYTES = KH * 2;     // 64 B: features (2 K-chunks) + bias (2 K-chunks)
-constexpr int L_ROW_BYTES = 16 * 2;     // 32 B: features only
+constexpr int L_ROW_BYTES = 16 * 2;     // 32 B: features only (mid and lo parts)
+// Operands are split in three fp16 parts v = hi + mid + lo (~33 significant
+// bits): H holds hi and the bias columns, M the mid parts, L the lo parts.
 constexpr int A_H_BYTES = QT * H_ROW_BYTES;       // 8 KB
+constexpr int A_M_BYTES = QT * L_ROW_BYTES;       // 4 KB
 constexpr int A_L_BYTES = QT * L_ROW_BYTES;       // 4 KB
-constexpr int A_TILE_BYTES = A_H_BYTES + A_L_BYTES;
-constexpr int A_BYTES = NQT * A_TILE_BYTES;       // 48 KB per unit
+constexpr int A_M_OFFSET = A_H_BYTES;
+constexpr int A_L_OFFSET = A_H_BYTES + A_M_BYTES;
+constexpr int A_TILE_BYTES = A_L_OFFSET + A_L_BYTES;  // 16 KB
+constexpr int A_BYTES = NQT * A_TILE_BYTES;       // 64 KB per unit
 constexpr int B_H_BYTES = NT * H_ROW_BYTES;       // 4 KB
+constexpr int B_M_BYTES = NT * L_ROW_BYTES;       // 2 KB
 constexpr int B_L_BYTES = NT * L_ROW_BYTES;       // 2 KB
-constexpr int B_X_OFFSET = B_H_BYTES + B_L_BYTES; // original FP32 rows, 64 B each
-constexpr int B_STAGE_BYTES = B_X_OFFSET + NT * FSK_D * 4;   // 10 KB
+constexpr int B_M_OFFSET = B_H_BYTES;
+constexpr int B_L_OFFSET = B_H_BYTES + B_M_BYTES;
+constexpr int B_X_OFFSET = B_L_OFFSET + B_L_BYTES; // original FP32 rows, 64 B each
+constexpr int B_STAGE_BYTES = B_X_OFFSET + NT * FSK_D * 4;   // 12 KB
 constexpr int EPI_WARPS = 4 * NQT;      // one warp per (TMEM lane quarter, query tile)
 constexpr int PRODUCER_WARP = EPI_WARPS;
-constexpr int MMA_WARP = EPI_WARPS + 1;
-constexpr int THREADS = (EPI_WARPS + 2) * 32;
+constexpr int MMA_WARP = EPI_WARPS + 1;   // owns TMEM, issues the MMAs of query tiles 0-1
+constexpr int MMA_WARP2 = EPI_WARPS + 2;  // issues the MMAs of query tiles 2-3
+constexpr int MMA_ISSUERS = 2;
+constexpr int THREADS = (EPI_WARPS + 3) * 32;
 constexpr int TMEM_COLS = 2 * NQT * NT; // double-buffered accumulators
 constexpr int SMEM_BYTES = A_BYTES + NS * B_STAGE_BYTES + 512;
-// A term is recomputed exactly when it exceeds this fraction of the running
-// sum of its query (including the current chunk's approximate sum).
-constexpr float NEAR_FRACTION = 1.0f / 64.0f;
+// A term is recomputed exactly when its 32-column chunk holds more than this
+// fraction of the running sum of its query (the chunk included).  With the
+// three-part operands the exponent of any other term is off by at most
+// ~2^-25 * 2 c2 |q - mu| |x - mu| (one FP32 rounding at the magnitude of the
+// cross product), so a term below an eighth of the sum moves it by well
+// under 1e-6.
+constexpr float NEAR_FRACTION = 1.0f / 8.0f;
 constexpr float FP16_TARGET = 8192.0f;  // largest operand magnitude aimed for
 
 static_assert(TMEM_COLS == 512, "TMEM budget");

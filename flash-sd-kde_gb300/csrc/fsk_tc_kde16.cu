@@ -11,29 +11,32 @@
 //    log2(e)/(2h^2), the log2-domain exponent of a pair is
 //        a2 = 2 c2 (q-mu).(x-mu) + beta_j + alpha_i,
 //    beta_j = -c2 |x_j-mu|^2, alpha_i = -c2 |q_i-mu|^2.
-//  * Operands are fp16 pairs v = hi + lo (22 significant bits): queries as
+//  * Operands are fp16 triples v = hi + mid + lo (~33 significant bits): queries as
 //    q' = 2 c2 (q-mu) 2^eq, data as x' = (x-mu) 2^ex with power-of-two
 //    scales chosen on the device so every operand stays in fp16 range and
 //    eq + ex = 0 (or the product is scaled down and multiplied back).  Each
 //    hi operand row carries 16 extra "bias" K-columns holding beta_j and
 //    alpha_i as three fp16 parts each against exact powers of two, so one
-//    accumulator D = hi.hi + hi.lo + lo.hi + bias.bias (four tcgen05.mma
-//    kind::f16, M=128, N=64, FP32 accumulation in tensor memory) *is* a2.
+//    accumulator D = mid.mid + hi.lo + lo.hi + hi.mid + mid.hi + hi.hi +
+//    bias.bias (seven tcgen05.mma kind::f16, M=128, N=64, FP32 accumulation
+//    in tensor memory) *is* a2, to one FP32 rounding at the magnitude of the
+//    cross product.
 //  * Epilogue: tcgen05.ld one query row per thread, 2^D on the SFU
 //    (ex2.approx), 32-column chunk sums, compensated (TwoSum) per query.
-//  * Exact near-pair recompute: when a 32-column chunk holds more than 1/64
+//  * Exact near-pair recompute: when a 32-column chunk holds more than 1/8
 //    of its query's running sum (carried across the data splits a CTA runs
 //    for that query block), the chunk's largest term is recomputed from
 //    direct FP32 differences of the original coordinates with the exponent
 //    product in double-float, and replaces its approximation.  The argmax
 //    rides in the low 5 mantissa bits, so all triggered lanes of a warp
-//    recompute one pair each in lock-step.  Other terms carry the ~2^-21
-//    relative error of the fp16x3 product, which averages out.
+//    recompute one pair each in lock-step.  Other terms carry the ~2^-25
+//    relative error of the accumulation, which averages out.
 //
-// Pipeline (one persistent CTA per SM, 18 warps):
+// Pipeline (one persistent CTA per SM, 19 warps):
 //   warp 16 : producer - bulk (TMA) copies of query images per unit and of
 //             data-tile images per stage into shared memory (mbarrier tx).
-//   warp 17 : owns TMEM (512 columns) and issues the MMAs (one lane).
+//   warps 17, 18 : issue the MMAs of query tiles 0-1 and 2-3 (one lane
+//             each); warp 17 owns TMEM (512 columns).
 //   warps 0-15: epilogue; warp w reads TMEM lanes 32*(w%4).. of query tile w/4.
 // A work unit is 512 queries (four M=128 tiles) x one data split; TMEM holds
 // two accumulator buffers x four query tiles x 64 columns.
@@ -68,15 +71,15 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
   if (threadIdx.x == 0) {
     for (int s = 0; s < NS; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1 + EPI_WARPS);
+      mbar_init(&empty[s], MMA_ISSUERS + EPI_WARPS);
     }
     for (int b = 0; b < 2; ++b) {
-      mbar_init(&tfull[b], 1);
+      mbar_init(&tfull[b], MMA_ISSUERS);
       mbar_init(&tempty[b], EPI_WARPS);
     }
     mbar_init(qready, 1);
-    mbar_init(qempty, 1);
-    mbar_init(drain, 1);
+    mbar_init(qempty, MMA_ISSUERS);
+    mbar_init(drain, MMA_ISSUERS);
     fence_barrier_init();
   }
   if (warp == MMA_WARP) {
@@ -115,9 +118,14 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
         }
       }
     }
-  } else if (warp == MMA_WARP) {
+  } else if (warp == MMA_WARP || warp == MMA_WARP2) {
+    // Two issuing threads, two query tiles each: one thread issuing all 28
+    // MMAs of a tile falls behind when it shares its scheduler with busy
+    // epilogue warps.  Each commits its own MMAs; the barriers they signal
+    // count one arrival per issuer.
     if (lane == 0) {
       const uint32_t idesc = idesc_f16_f32(QT, NT);
+      const int a0 = (warp == MMA_WARP) ? 0 : NQT / 2;
       int64_t g = 0, k = 0;
       for (int64_t u = u_begin; u < u_end; ++u, ++k) {
         const int64_t sp = u % p.splits;
@@ -131,20 +139,15 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
           if (!mbar_wait(&tempty[b], (uint32_t)(((g >> 1) & 1) ^ 1), 5)) goto done;
           tc_fence_after();
           const uint32_t bs = smem_u32(sB + s * B_STAGE_BYTES);
-          const uint64_t b_hf = smem_desc_kmajor(bs, 128, 8 * H_ROW_BYTES);
-          const uint64_t b_hb = smem_desc_kmajor(bs + 256, 128, 8 * H_ROW_BYTES);
-          const uint64_t b_l = smem_desc_kmajor(bs + B_H_BYTES, 128, 8 * L_ROW_BYTES);
+          const uint64_t b_h = smem_desc_kmajor(bs, 128, 8 * H_ROW_BYTES);
+          const uint64_t b_m = smem_desc_kmajor(bs + B_M_OFFSET, 128, 8 * L_ROW_BYTES);
+          const uint64_t b_l = smem_desc_kmajor(bs + B_L_OFFSET, 128, 8 * L_ROW_BYTES);
 #pragma unroll
-          for (int a = 0; a < NQT; ++a) {
+          for (int a = a0; a < a0 + NQT / 2; ++a) {
             const uint32_t as = smem_u32(sA + a * A_TILE_BYTES);
-            const uint64_t a_hf = smem_desc_kmajor(as, 128, 8 * H_ROW_BYTES);
-            const uint64_t a_hb = smem_desc_kmajor(as + 256, 128, 8 * H_ROW_BYTES);
-            const uint64_t a_l = smem_desc_kmajor(as + A_H_BYTES, 128, 8 * L_ROW_BYTES);
-            const uint32_t d = tmem_base + (uint32_t)(b * (NQT * NT) + a * NT);
-            mma_f16_ss(d, a_l, b_hf, idesc, 0u);   // lo . hi
-            mma_f16_ss(d, a_hf, b_l, idesc, 1u);   // hi . lo
-            mma_f16_ss(d, a_hf, b_hf, idesc, 1u);  // hi . hi
-            mma_f16_ss(d, a_hb, b_hb, idesc, 1u);  // beta_j + alpha_i
+            mma_s_tile(tmem_base + (uint32_t)(b * (NQT * NT) + a * NT), smem_desc_kmajor(as, 128, 8 * H_ROW_BYTES),
+                       smem_desc_kmajor(as + A_M_OFFSET, 128, 8 * L_ROW_BYTES),
+                       smem_desc_kmajor(as + A_L_OFFSET, 128, 8 * L_ROW_BYTES), b_h, b_m, b_l, idesc);
           }
           mma_commit(&tfull[b]);
           mma_commit(&empty[s]);
@@ -295,8 +298,8 @@ done:
       mbar_wait(&full[i % NS], (uint32_t)((i / NS) & 1), 7);
     if (n_query_copies > 0) mbar_wait(qready, (uint32_t)((n_query_copies - 1) & 1), 8);
   }
-  if (warp == MMA_WARP && lane == 0) {
-    mma_commit(drain);
+  if ((warp == MMA_WARP || warp == MMA_WARP2) && lane == 0) {
+    mma_commit(drain);   // one arrival per issuing thread, when its MMAs have finished
     mbar_wait(drain, 0, 9);
   }
   tc_fence_before();
@@ -393,7 +396,8 @@ __global__ void prep_data_kernel(const float* __restrict__ x, int64_t n, int64_t
   uint8_t* tile = img + (j / NT) * (int64_t)B_STAGE_BYTES;
   const int r = (int)(j % NT);
   const float beta = ok ? -c2 * nrm * sc->b_scale : 0.f;
-  write_operand_row(tile, tile + B_H_BYTES, r, v, beta, ok ? ldexpf(1.f, sc->pad[0]) : 0.f, true);
+  write_operand_row(tile, tile + B_M_OFFSET, tile + B_L_OFFSET, r, v, beta, ok ? ldexpf(1.f, sc->pad[0]) : 0.f,
+                    true);
   float4* xr = reinterpret_cast<float4*>(tile + B_X_OFFSET + r * (FSK_D * 4));
 #pragma unroll
   for (int k = 0; k < 4; ++k) xr[k] = make_float4(xo[4 * k], xo[4 * k + 1], xo[4 * k + 2], xo[4 * k + 3]);
@@ -420,7 +424,8 @@ __global__ void prep_query_kernel(const float* __restrict__ q, int64_t m, int64_
   }
   uint8_t* tile = img + (i / QT) * (int64_t)A_TILE_BYTES;
   const float alpha = ok ? (alpha_off - c2 * nrm) * sc->a_scale : 0.f;
-  write_operand_row(tile, tile + A_H_BYTES, (int)(i % QT), v, alpha, ok ? ldexpf(1.f, sc->pad[1]) : 0.f, false);
+  write_operand_row(tile, tile + A_M_OFFSET, tile + A_L_OFFSET, (int)(i % QT), v, alpha,
+                    ok ? ldexpf(1.f, sc->pad[1]) : 0.f, false);
 #pragma unroll
   for (int k = 0; k < FSK_D; ++k) qexact[i * FSK_D + k] = qo[k];
 }

@@ -1,7 +1,8 @@
 // fsk_tc_ops.cuh - device helpers shared by the tcgen05 kernels: fp16
 // instruction descriptors and MMA issue, the fp16 operand-image writers
-// (core-matrix layout, hi/lo parts and the bias columns that fold the norm
-// terms into the accumulator) and the exact direct-difference distance.
+// (core-matrix layout, hi/mid/lo parts and the bias columns that fold the
+// norm terms into the accumulator), the six-product S MMA sequence and the
+// exact direct-difference distance.
 #pragma once
 #include <cuda_fp16.h>
 
@@ -20,6 +21,22 @@ __host__ __device__ constexpr uint32_t idesc_f16_f32(int M, int N) {
 __device__ __forceinline__ void mma_f16_ss(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc,
                                            uint32_t idesc, uint32_t accumulate) {
   mma_bf16_ss(d_tmem, a_desc, b_desc, idesc, accumulate);  // same instruction, kind::f16
+}
+
+// D = a2 for one 128-query tile x one data tile: the six products of the
+// three-part operands whose error terms exceed ~2^-33 (smallest first, so
+// the large hi.hi and bias terms meet last), then the bias K step.
+// a_h / b_h: H images (hi | bias), a_m / b_m, a_l / b_l: mid and lo images.
+__device__ __forceinline__ void mma_s_tile(uint32_t d, uint64_t a_h, uint64_t a_m, uint64_t a_l, uint64_t b_h,
+                                           uint64_t b_m, uint64_t b_l, uint32_t idesc) {
+  const uint64_t bias = 256 >> 4;   // bias K step: +256 B in the start-address field
+  mma_f16_ss(d, a_m, b_m, idesc, 0u);       // mid . mid
+  mma_f16_ss(d, a_h, b_l, idesc, 1u);       // hi . lo
+  mma_f16_ss(d, a_l, b_h, idesc, 1u);       // lo . hi
+  mma_f16_ss(d, a_h, b_m, idesc, 1u);       // hi . mid
+  mma_f16_ss(d, a_m, b_h, idesc, 1u);       // mid . hi
+  mma_f16_ss(d, a_h, b_h, idesc, 1u);       // hi . hi
+  mma_f16_ss(d, a_h + bias, b_h + bias, idesc, 1u);   // beta_j + alpha_i
 }
 
 // sum_k (q_k - x_k)^2 from the original FP32 coordinates of data row r.
@@ -51,16 +68,19 @@ __device__ __forceinline__ void put_h(uint8_t* img, int r, int k, int row_bytes,
   *reinterpret_cast<__half*>(img + cm_offset(r, k, row_bytes)) = v;
 }
 
-// Writes one operand row: H image (features hi + 16 bias columns) and L
-// image (features lo).  bias_own: three parts of this row's own norm term;
-// pow_other: the exact power of two multiplying the other side's parts.
-__device__ __forceinline__ void write_operand_row(uint8_t* h_img, uint8_t* l_img, int r, const float (&v)[FSK_D],
-                                                  float own_term, float pow_other, bool own_first) {
+// Writes one operand row: H image (features hi + 16 bias columns), M image
+// (features mid) and L image (features lo), v = hi + mid + lo.  own_term:
+// this row's norm term, as three parts in its bias columns; pow_other: the
+// exact power of two multiplying the other side's parts.
+__device__ __forceinline__ void write_operand_row(uint8_t* h_img, uint8_t* m_img, uint8_t* l_img, int r,
+                                                  const float (&v)[FSK_D], float own_term, float pow_other,
+                                                  bool own_first) {
 #pragma unroll
   for (int k = 0; k < FSK_D; ++k) {
-    const __half hi = __float2half_rn(v[k]);
-    const __half lo = __float2half_rn(v[k] - __half2float(hi));
+    __half hi, mid, lo;
+    split3_f16(v[k], hi, mid, lo);
     put_h(h_img, r, k, H_ROW_BYTES, hi);
+    put_h(m_img, r, k, L_ROW_BYTES, mid);
     put_h(l_img, r, k, L_ROW_BYTES, lo);
   }
   __half p0, p1, p2;

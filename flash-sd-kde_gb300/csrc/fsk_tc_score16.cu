@@ -10,8 +10,8 @@
 // centred (sum_j phi_ij (x_j - mu)) and mu * pdf_sum is added back in FP64.
 //
 // How (per 128-query x 64-point tile):
-//  * S = the log2-domain exponent a2 + 15, from the same fp16 hi/lo + bias
-//    operand images and four tcgen05.mma as the KDE kernel (fsk_tc_kde16.cu);
+//  * S = the log2-domain exponent a2 + 15, from the same three-part fp16 +
+//    bias operand images and seven tcgen05.mma as the KDE kernel (fsk_tc_kde16.cu);
 //    the +15 rides in the query's bias term, so 2^S = phi * 2^15 and the
 //    weights keep fp16 normal range down to phi ~ 2^-29.
 //  * Epilogue: tcgen05.ld, ex2.approx, pdf chunk sums, the exact near-pair
@@ -26,9 +26,10 @@
 //    from the data stage, N = 32, FP32 accumulation over a group of S_GROUP
 //    tiles, then added into compensated FP32 sums.
 //
-// Pipeline (one persistent CTA per SM, 19 warps):
+// Pipeline (one persistent CTA per SM, 20 warps):
 //   warp 16 : producer (bulk copies of query images per unit, data stages).
-//   warp 17 : owns TMEM; issues S up to NBUF tiles ahead of W (one lane).
+//   warps 17, 19 : issue S for query tiles 0 and 1 (one lane each), up to
+//             NBUF tiles ahead of W; warp 17 owns TMEM.
 //   warp 18 : issues the weighted-sum MMAs (one lane).  An M=128, K=16
 //             tcgen05.mma costs ~46 cycles whatever N <= 64 is, so this
 //             product is the expensive part: two N=32 MMAs per K step, and
@@ -51,19 +52,20 @@ namespace tc {
 namespace {
 
 constexpr int SNQT = 2;                                    // query tiles per unit (256 queries)
-constexpr int SNS = 6;                                     // data stages
+constexpr int SNS = 5;                                     // data stages
 constexpr int XT_ROW_BYTES = NT * 2;                       // one feature row over 64 points, fp16
 constexpr int XT_BYTES = FSK_D * XT_ROW_BYTES;             // 2 KB
-constexpr int S_XTH_OFFSET = B_H_BYTES + B_L_BYTES;        // 6 KB
-constexpr int S_XTL_OFFSET = S_XTH_OFFSET + XT_BYTES;      // 8 KB
-constexpr int S_X_OFFSET = S_XTL_OFFSET + XT_BYTES;        // 10 KB: original FP32 rows
-constexpr int S_STAGE_BYTES = S_X_OFFSET + NT * FSK_D * 4; // 14 KB
-constexpr int S_A_BYTES = SNQT * A_TILE_BYTES;             // 24 KB
+constexpr int S_XTH_OFFSET = B_L_OFFSET + B_L_BYTES;       // 8 KB
+constexpr int S_XTL_OFFSET = S_XTH_OFFSET + XT_BYTES;      // 10 KB
+constexpr int S_X_OFFSET = S_XTL_OFFSET + XT_BYTES;        // 12 KB: original FP32 rows
+constexpr int S_STAGE_BYTES = S_X_OFFSET + NT * FSK_D * 4; // 16 KB
+constexpr int S_A_BYTES = SNQT * A_TILE_BYTES;             // 32 KB
 constexpr int S_EPI_WARPS = 8 * SNQT;
 constexpr int S_PRODUCER_WARP = S_EPI_WARPS;
-constexpr int S_MMA_WARP = S_EPI_WARPS + 1;     // issues the S MMAs, owns TMEM
+constexpr int S_MMA_WARP = S_EPI_WARPS + 1;     // issues the S MMAs of query tile 0, owns TMEM
 constexpr int W_MMA_WARP = S_EPI_WARPS + 2;     // issues the weighted-sum MMAs
-constexpr int S_THREADS = (S_EPI_WARPS + 3) * 32;
+constexpr int S_MMA_WARP2 = S_EPI_WARPS + 3;    // issues the S MMAs of query tile 1
+constexpr int S_THREADS = (S_EPI_WARPS + 4) * 32;
 constexpr int S_GROUP = 8;                                 // data tiles per W accumulation
 constexpr int NBUF = 3;                                    // S / weight buffers in TMEM
 constexpr int WN = 2 * FSK_D;                              // W MMA N: X_hi and X_lo rows
@@ -169,17 +171,17 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
   if (threadIdx.x == 0) {
     for (int s = 0; s < SNS; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1 + S_EPI_WARPS);
+      mbar_init(&empty[s], 1 + S_EPI_WARPS);   // the W thread's commit + every epilogue warp
     }
-    for (int b = 0; b < NBUF; ++b) mbar_init(&tfull[b], 1);
+    for (int b = 0; b < NBUF; ++b) mbar_init(&tfull[b], 2);   // one commit per S thread
     for (int b = 0; b < 2; ++b) {
       mbar_init(&wfull[b], 1);
       mbar_init(&wempty[b], S_EPI_WARPS);
     }
     for (int i = 0; i < NBUF * SNQT; ++i) mbar_init(&pready[i], 8);
     mbar_init(qready, 1);
-    mbar_init(qempty, 1 + S_EPI_WARPS);   // last S MMA of the unit + every epilogue warp
-    mbar_init(drain, 2);
+    mbar_init(qempty, 2 + S_EPI_WARPS);   // last S MMAs of the unit (both S threads) + every epilogue warp
+    mbar_init(drain, 3);
     mbar_init(cready, S_EPI_WARPS);
     fence_barrier_init();
   }
@@ -218,7 +220,7 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
         }
       }
     }
-  } else if (warp == S_MMA_WARP) {
+  } else if (warp == S_MMA_WARP || warp == S_MMA_WARP2) {
     // S(g) for every tile, up to NBUF tiles ahead of the W MMAs: buffer
     // g % NBUF is reused once W(g - NBUF) has read its weights, which the
     // stage barrier of tile g - NBUF signals (it completes with the W
@@ -227,19 +229,21 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
     // earlier MMA of its thread: waiting for W(g - NBUF) from one issuing
     // thread would also wait for the S MMAs issued after it and drain the
     // tensor pipe every tile.
+    // Two S threads, one query tile each (one thread issuing all 14 S MMAs of
+    // a tile falls behind when it shares its scheduler with busy warps).
     if (lane == 0) {
+      const int a_mine = warp == S_MMA_WARP ? 0 : 1;
       const uint32_t idesc_s = idesc_f16_f32(QT, NT);
-      uint64_t a_hf[SNQT], a_hb[SNQT], a_l[SNQT];
-#pragma unroll
-      for (int a = 0; a < SNQT; ++a) {
-        const uint32_t as = smem_u32(sA + a * A_TILE_BYTES);
-        a_hf[a] = smem_desc_kmajor(as, 128, 8 * H_ROW_BYTES);
-        a_hb[a] = a_hf[a] + (256 >> 4);   // bias K step (start-address field, no carry below 2^18 B)
-        a_l[a] = smem_desc_kmajor(as + A_H_BYTES, 128, 8 * L_ROW_BYTES);
-      }
+      // descriptors are advanced by adding (bytes >> 4) to the start-address
+      // field (shared addresses stay below 2^18 B, so the field cannot carry)
+      const uint32_t as = smem_u32(sA + a_mine * A_TILE_BYTES);
+      const uint64_t a_h = smem_desc_kmajor(as, 128, 8 * H_ROW_BYTES);
+      const uint64_t a_m = smem_desc_kmajor(as + A_M_OFFSET, 128, 8 * L_ROW_BYTES);
+      const uint64_t a_l = smem_desc_kmajor(as + A_L_OFFSET, 128, 8 * L_ROW_BYTES);
       const uint32_t b0 = smem_u32(sB);
       const uint64_t dh0 = smem_desc_kmajor(b0, 128, 8 * H_ROW_BYTES);
-      const uint64_t dl0 = smem_desc_kmajor(b0 + B_H_BYTES, 128, 8 * L_ROW_BYTES);
+      const uint64_t dm0 = smem_desc_kmajor(b0 + B_M_OFFSET, 128, 8 * L_ROW_BYTES);
+      const uint64_t dl0 = smem_desc_kmajor(b0 + B_L_OFFSET, 128, 8 * L_ROW_BYTES);
       TileCursor cs;
       cs.start((int)u_begin, (int)u_end, (int)p.splits, (int)p.tiles_per_split, (int)p.n_tiles);
       int gs = 0, kq = 0;
@@ -254,16 +258,8 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
         if (!mbar_wait(&full[s], (uint32_t)((gs / SNS) & 1), 24)) goto done;
         tc_fence_after();
         const uint64_t so = (uint64_t)((s * S_STAGE_BYTES) >> 4);
-        const uint64_t b_hf = dh0 + so, b_hb = dh0 + so + (256 >> 4), b_l = dl0 + so;
         const uint32_t d0 = tmem_base + (uint32_t)(T_S + (gs % NBUF) * (SNQT * NT));
-#pragma unroll
-        for (int a = 0; a < SNQT; ++a) {
-          const uint32_t d = d0 + (uint32_t)(a * NT);
-          mma_f16_ss(d, a_l[a], b_hf, idesc_s, 0u);
-          mma_f16_ss(d, a_hf[a], b_l, idesc_s, 1u);
-          mma_f16_ss(d, a_hf[a], b_hf, idesc_s, 1u);
-          mma_f16_ss(d, a_hb[a], b_hb, idesc_s, 1u);
-        }
+        mma_s_tile(d0 + (uint32_t)(a_mine * NT), a_h, a_m, a_l, dh0 + so, dm0 + so, dl0 + so, idesc_s);
         mma_commit(&tfull[gs % NBUF]);
         if (cs.t == cs.t1 - 1) mma_commit(qempty);   // last S read of this unit's query images
         ++gs;
@@ -548,7 +544,7 @@ done:
       mbar_wait(&full[i % SNS], (uint32_t)((i / SNS) & 1), 32);
     if (n_query_copies > 0) mbar_wait(qready, (uint32_t)((n_query_copies - 1) & 1), 33);
   }
-  if ((warp == S_MMA_WARP || warp == W_MMA_WARP) && lane == 0) {
+  if ((warp == S_MMA_WARP || warp == S_MMA_WARP2 || warp == W_MMA_WARP) && lane == 0) {
     mma_commit(drain);   // one arrival per issuing thread, when its MMAs have finished
     mbar_wait(drain, 0, 34);
   }
@@ -558,8 +554,8 @@ done:
   if (warp == S_MMA_WARP) tmem_dealloc(tmem_base, S_TMEM_COLS);
 }
 
-// Data stage image: [H (64 x 32 fp16) | L (64 x 16 fp16) | XT hi (16 x 64 fp16)
-// | XT lo | x (64 x 16 FP32)].  XT rows are features, K-major over the points.
+// Data stage image: [H (64 x 32 fp16) | M (64 x 16 fp16) | L (64 x 16 fp16)
+// | XT hi (16 x 64 fp16) | XT lo | x (64 x 16 FP32)].  XT rows are features, K-major over the points.
 __global__ void prep_score_data_kernel(const float* __restrict__ x, int64_t n, int64_t n_pad,
                                        const float* __restrict__ mu, float c2,
                                        const TcScales* __restrict__ sc, uint8_t* __restrict__ img) {
@@ -584,7 +580,8 @@ __global__ void prep_score_data_kernel(const float* __restrict__ x, int64_t n, i
     put_h(tile + S_XTL_OFFSET, k, r, XT_ROW_BYTES, wl);
   }
   const float beta = ok ? -c2 * nrm * sc->b_scale : 0.f;
-  write_operand_row(tile, tile + B_H_BYTES, r, v, beta, ok ? ldexpf(1.f, sc->pad[0]) : 0.f, true);
+  write_operand_row(tile, tile + B_M_OFFSET, tile + B_L_OFFSET, r, v, beta, ok ? ldexpf(1.f, sc->pad[0]) : 0.f,
+                    true);
   float4* xr = reinterpret_cast<float4*>(tile + S_X_OFFSET + r * (FSK_D * 4));
 #pragma unroll
   for (int k = 0; k < 4; ++k) xr[k] = make_float4(xo[4 * k], xo[4 * k + 1], xo[4 * k + 2], xo[4 * k + 3]);
