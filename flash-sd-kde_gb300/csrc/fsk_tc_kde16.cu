@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
 #pragma unroll
           for (int a = a0; a < a0 + NQT / 2; ++a) {
             const uint32_t as = smem_u32(sA + a * A_TILE_BYTES);
-            mma_s_tile(tmem_base + (uint32_t)(b * (NQT * NT) + a * NT), smem_desc_kmajor(as, 128, 8 * H_ROW_BYTES),
+            mma_s_tile<true>(tmem_base + (uint32_t)(b * (NQT * NT) + a * NT), smem_desc_kmajor(as, 128, 8 * H_ROW_BYTES),
                        smem_desc_kmajor(as + A_M_OFFSET, 128, 8 * L_ROW_BYTES),
                        smem_desc_kmajor(as + A_L_OFFSET, 128, 8 * L_ROW_BYTES), b_h, b_m, b_l, idesc);
           }

@@ -10,8 +10,8 @@
 // centred (sum_j phi_ij (x_j - mu)) and mu * pdf_sum is added back in FP64.
 //
 // How (per 128-query x 64-point tile):
-//  * S = the log2-domain exponent a2 + 15, from the same three-part fp16 +
-//    bias operand images and seven tcgen05.mma as the KDE kernel (fsk_tc_kde16.cu);
+//  * S = the log2-domain exponent a2 + 15, from the operand images of the KDE
+//    kernel (fsk_tc_kde16.cu), two-part product: four tcgen05.mma;
 //    the +15 rides in the query's bias term, so 2^S = phi * 2^15 and the
 //    weights keep fp16 normal range down to phi ~ 2^-29.
 //  * Epilogue: tcgen05.ld, ex2.approx, pdf chunk sums, the exact near-pair
@@ -87,6 +87,10 @@ constexpr int S_WACC_BYTES = 4 * S_EPI_WARPS * 32 * 16;                // 32 KB
 constexpr int S_MU_OFFSET = S_WACC_OFFSET + S_WACC_BYTES;             // data mean, 16 FP32
 constexpr int S_SMEM_BYTES = S_MU_OFFSET + FSK_D * 4;
 constexpr float PHI_LOG2_SCALE = 15.0f;                    // weights are phi * 2^15
+// The S product here is the two-part one (four MMAs: this kernel is bound by
+// the tensor core's per-instruction cost), whose exponent error is ~8x the
+// three-part one's, so the near-pair threshold is 1/64 of the running sum.
+constexpr float SCORE_NEAR_FRACTION = 1.0f / 64.0f;
 static_assert(T_W + 2 * SNQT * WN <= S_TMEM_COLS, "TMEM budget");
 static_assert(S_XTL_OFFSET == S_XTH_OFFSET + 16 * XT_ROW_BYTES, "X_lo rows follow X_hi rows (one N=32 operand)");
 static_assert(S_STAGE_BYTES % 16 == 0 && S_A_BYTES % 16 == 0 && S_QX_BYTES % 16 == 0, "bulk copy granularity");
@@ -259,7 +263,7 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
         tc_fence_after();
         const uint64_t so = (uint64_t)((s * S_STAGE_BYTES) >> 4);
         const uint32_t d0 = tmem_base + (uint32_t)(T_S + (gs % NBUF) * (SNQT * NT));
-        mma_s_tile(d0 + (uint32_t)(a_mine * NT), a_h, a_m, a_l, dh0 + so, dm0 + so, dl0 + so, idesc_s);
+        mma_s_tile<false>(d0 + (uint32_t)(a_mine * NT), a_h, a_m, a_l, dh0 + so, dm0 + so, dl0 + so, idesc_s);
         mma_commit(&tfull[gs % NBUF]);
         if (cs.t == cs.t1 - 1) mma_commit(qempty);   // last S read of this unit's query images
         ++gs;
@@ -393,7 +397,7 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
         }
         pa = __fadd2_rn(pa, pb);
         const float cs = pa.x + pa.y;
-        const bool trig = cs > (s_carry + acc.s + cs) * NEAR_FRACTION;
+        const bool trig = cs > (s_carry + acc.s + cs) * SCORE_NEAR_FRACTION;
         if (__any_sync(0xffffffffu, trig)) {
           // The chunk's largest weight is recomputed exactly (argmax on keys
           // = value bits with the column in the low 5 bits, as in the KDE
