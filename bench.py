@@ -53,9 +53,10 @@ KERNEL_NAMES = {1: "kde16_tc_kernel", 2: "kde16_simt_kernel", 3: "score16_simt_k
                 4: "score16_sym_simt_kernel", 5: "kde1d_kernel", 6: "kde1d_score_kernel",
                 7: "score16_tc_kernel"}
 # fp16 tensor-core flops per pair evaluation issued by the tcgen05 kernels:
-# KDE: 4 MMAs (M=128, N=64, K=16) per 128x64 pairs; score: the same S
-# product plus 16 MMAs (M=128, N=32, K=16) per 256x64 pairs.
-MMA_FLOPS_PER_PAIR = {"kde16_tc_kernel": 4 * 2 * 16, "score16_tc_kernel": 4 * 2 * 16 + 16 * 2 * 128 * 32 * 16 / (256 * 64)}
+# KDE: 7 MMAs (M=128, N=128, K=16; three-part operands) per 128x128 pairs;
+# score: 4 MMAs (M=128, N=64, K=16; two-part operands) per 128x64 pairs plus
+# 16 MMAs (M=128, N=32, K=16) per 256x64 pairs for the weighted sum.
+MMA_FLOPS_PER_PAIR = {"kde16_tc_kernel": 7 * 2 * 16, "score16_tc_kernel": 4 * 2 * 16 + 16 * 2 * 128 * 32 * 16 / (256 * 64)}
 
 
 def parse():

@@ -150,7 +150,7 @@ int fsk_kde16(const float* queries, int64_t m, const float* data, int64_t n, dou
     launch_mean16(data, n, cb.scratch, cb.mu, cb.mu64, s);
     st = tc::launch_kde16_tc(queries, m, data, n, cb.mu, bandwidth, laplace, p.tcp, c, &part, p.atomic, s);
     if (st) return st;
-    splits = p.atomic ? 1 : (int)p.tcp.splits;
+    splits = p.atomic ? 1 : (int)p.tcp.part_rows;
   }
   launch_reduce_rows(part, splits, m, out_scale, out_eps, (flags & FSK_OUT_LOG) != 0, out, s);
   return cuda_status(cudaGetLastError());

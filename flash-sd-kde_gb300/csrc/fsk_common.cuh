@@ -201,16 +201,30 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
 // records FSK_ERR_DEVICE_TIMEOUT (with the call-site id) and returns false.
 // (The error word is not consulted here: a stale error from an earlier,
 // unacknowledged launch must not cut short the waits of a later one.)
+// After the first probe the thread waits with a suspend-time hint of 50 us:
+// it sleeps until the phase completes (or the hint runs out) instead of
+// spinning, so a waiting warp takes no issue slots from the busy warps of
+// its scheduler.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(50000u)
+      : "memory");
+  return ok != 0;
+}
+
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned int site) {
   if (mbar_try_wait(bar, parity)) return true;
-  uint64_t t0 = globaltimer_ns();
-  for (uint32_t it = 0;; ++it) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if ((it & 1023u) == 1023u) {
-      if (globaltimer_ns() - t0 > 2000000000ull) {
-        record_error(FSK_ERR_DEVICE_TIMEOUT, site);
-        return false;
-      }
+  const uint64_t t0 = globaltimer_ns();
+  for (;;) {
+    if (mbar_try_wait_sleep(bar, parity)) return true;
+    if (globaltimer_ns() - t0 > 2000000000ull) {
+      record_error(FSK_ERR_DEVICE_TIMEOUT, site);
+      return false;
     }
   }
 }

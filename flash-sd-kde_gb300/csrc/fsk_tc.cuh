@@ -7,9 +7,13 @@ namespace tc {
 
 // ---- geometry -----------------------------------------------------------------
 constexpr int QT = 128;                 // queries per MMA tile (M, one TMEM lane each)
-constexpr int NQT = 4;                  // query tiles per work unit (512 queries)
-constexpr int NT = 64;                  // data points per stage (MMA N)
-constexpr int NS = 8;                   // shared-memory data stages
+constexpr int NT = 64;                  // data points per 64-row operand image (score kernel stages)
+// KDE kernel: 2 query tiles x 128 data points per tile (an M=128, K=16 MMA
+// costs ~46 cycles for any N <= 64 and 64 cycles at N = 128, so N = 128
+// halves the instruction count of the S product per pair).
+constexpr int NQT = 2;                  // KDE: query tiles per work unit (256 queries)
+constexpr int KNT = 128;                // KDE: data points per stage (MMA N)
+constexpr int NS = 6;                   // KDE: shared-memory data stages
 constexpr int KH = 32;                  // K of the "hi" operand: 16 features + 16 bias columns
 // Operand images, fp16, no-swizzle K-major core-matrix layout: 8-row groups,
 // each group = (K/8) core matrices of 8 rows x 16 B stored back to back.
@@ -23,22 +27,28 @@ constexpr int A_L_BYTES = QT * L_ROW_BYTES;       // 4 KB
 constexpr int A_M_OFFSET = A_H_BYTES;
 constexpr int A_L_OFFSET = A_H_BYTES + A_M_BYTES;
 constexpr int A_TILE_BYTES = A_L_OFFSET + A_L_BYTES;  // 16 KB
-constexpr int A_BYTES = NQT * A_TILE_BYTES;       // 64 KB per unit
+constexpr int A_BYTES = NQT * A_TILE_BYTES;       // 32 KB per KDE unit
 constexpr int B_H_BYTES = NT * H_ROW_BYTES;       // 4 KB
 constexpr int B_M_BYTES = NT * L_ROW_BYTES;       // 2 KB
 constexpr int B_L_BYTES = NT * L_ROW_BYTES;       // 2 KB
 constexpr int B_M_OFFSET = B_H_BYTES;
 constexpr int B_L_OFFSET = B_H_BYTES + B_M_BYTES;
 constexpr int B_X_OFFSET = B_L_OFFSET + B_L_BYTES; // original FP32 rows, 64 B each
-constexpr int B_STAGE_BYTES = B_X_OFFSET + NT * FSK_D * 4;   // 12 KB
-constexpr int EPI_WARPS = 4 * NQT;      // one warp per (TMEM lane quarter, query tile)
+// KDE data stage: [H (128 x 32 fp16) | M (128 x 16) | L (128 x 16) | x (128 x 16 FP32)]
+constexpr int KB_H_BYTES = KNT * H_ROW_BYTES;                 // 8 KB
+constexpr int KB_M_OFFSET = KB_H_BYTES;
+constexpr int KB_L_OFFSET = KB_M_OFFSET + KNT * L_ROW_BYTES;  // 12 KB
+constexpr int KB_X_OFFSET = KB_L_OFFSET + KNT * L_ROW_BYTES;  // 16 KB
+constexpr int KB_STAGE_BYTES = KB_X_OFFSET + KNT * FSK_D * 4; // 24 KB
+constexpr int EPI_WARPS = 8 * NQT;      // KDE: (lane quarter, column half) per query tile
 constexpr int PRODUCER_WARP = EPI_WARPS;
-constexpr int MMA_WARP = EPI_WARPS + 1;   // owns TMEM, issues the MMAs of query tiles 0-1
-constexpr int MMA_WARP2 = EPI_WARPS + 2;  // issues the MMAs of query tiles 2-3
+constexpr int MMA_WARP = EPI_WARPS + 1;   // owns TMEM, issues the MMAs of query tile 0
+constexpr int MMA_WARP2 = EPI_WARPS + 2;  // issues the MMAs of query tile 1
 constexpr int MMA_ISSUERS = 2;
 constexpr int THREADS = (EPI_WARPS + 3) * 32;
-constexpr int TMEM_COLS = 2 * NQT * NT; // double-buffered accumulators
-constexpr int SMEM_BYTES = A_BYTES + NS * B_STAGE_BYTES + 512;
+constexpr int TMEM_COLS = 2 * NQT * KNT; // double-buffered accumulators
+constexpr int K_BAR_OFFSET = A_BYTES + NS * KB_STAGE_BYTES;
+constexpr int SMEM_BYTES = K_BAR_OFFSET + 256;
 // A term is recomputed exactly when its 32-column chunk holds more than this
 // fraction of the running sum of its query (the chunk included).  With the
 // three-part operands the exponent of any other term is off by at most
@@ -49,7 +59,8 @@ constexpr float NEAR_FRACTION = 1.0f / 8.0f;
 constexpr float FP16_TARGET = 8192.0f;  // largest operand magnitude aimed for
 
 static_assert(TMEM_COLS == 512, "TMEM budget");
-static_assert(B_STAGE_BYTES % 16 == 0 && A_BYTES % 16 == 0, "bulk copy granularity");
+static_assert(KB_STAGE_BYTES % 16 == 0 && A_BYTES % 16 == 0, "bulk copy granularity");
+static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
 
 // Device-side scale state written by the prep kernels (see fsk_tc_kde16.cu).
 struct TcScales {
@@ -79,6 +90,7 @@ struct TcParams {
 
 struct TcPlan {
   int64_t m_pad, n_pad, n_tiles, q_blocks, splits, tiles_per_split;
+  int64_t part_rows;   // FP64 partial rows per query written by the kernel
   int grid;
 };
 

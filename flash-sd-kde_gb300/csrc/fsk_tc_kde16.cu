@@ -18,7 +18,7 @@
 //    hi operand row carries 16 extra "bias" K-columns holding beta_j and
 //    alpha_i as three fp16 parts each against exact powers of two, so one
 //    accumulator D = mid.mid + hi.lo + lo.hi + hi.mid + mid.hi + hi.hi +
-//    bias.bias (seven tcgen05.mma kind::f16, M=128, N=64, FP32 accumulation
+//    bias.bias (seven tcgen05.mma kind::f16, M=128, N=128, FP32 accumulation
 //    in tensor memory) *is* a2, to one FP32 rounding at the magnitude of the
 //    cross product.
 //  * Epilogue: tcgen05.ld one query row per thread, 2^D on the SFU
@@ -26,20 +26,25 @@
 //  * Exact near-pair recompute: when a 32-column chunk holds more than 1/8
 //    of its query's running sum (carried across the data splits a CTA runs
 //    for that query block), the chunk's largest term is recomputed from
-//    direct FP32 differences of the original coordinates with the exponent
-//    product in double-float, and replaces its approximation.  The argmax
-//    rides in the low 5 mantissa bits, so all triggered lanes of a warp
-//    recompute one pair each in lock-step.  Other terms carry the ~2^-25
-//    relative error of the accumulation, which averages out.
+//    direct FP32 differences of the original coordinates (kept in the data
+//    stage) with the exponent product in double-float, and replaces its
+//    approximation.  The argmax rides in the low 5 mantissa bits, so all
+//    triggered lanes of a warp recompute one pair each in lock-step.  Other
+//    terms carry the ~2^-25 relative error of the accumulation, which
+//    averages out.
 //
 // Pipeline (one persistent CTA per SM, 19 warps):
 //   warp 16 : producer - bulk (TMA) copies of query images per unit and of
-//             data-tile images per stage into shared memory (mbarrier tx).
-//   warps 17, 18 : issue the MMAs of query tiles 0-1 and 2-3 (one lane
-//             each); warp 17 owns TMEM (512 columns).
-//   warps 0-15: epilogue; warp w reads TMEM lanes 32*(w%4).. of query tile w/4.
-// A work unit is 512 queries (four M=128 tiles) x one data split; TMEM holds
-// two accumulator buffers x four query tiles x 64 columns.
+//             data-tile images (128 points) per stage into shared memory
+//             (mbarrier tx).
+//   warps 17, 18 : issue the MMAs of query tiles 0 and 1 (one lane each);
+//             warp 17 owns TMEM (512 columns).
+//   warps 0-15: epilogue; warp w reads TMEM lanes 32*(w%4).. and columns
+//             64*((w/4)%2).. of query tile w/8.
+// A work unit is 256 queries (two M=128 tiles) x one data split; TMEM holds
+// two accumulator buffers x two query tiles x 128 columns.  Each query's sum
+// is kept as two column halves by two threads and written as two FP64
+// partial rows per split.
 #include <cuda_fp16.h>
 
 #include "fsk_kernels.cuh"
@@ -52,18 +57,18 @@ namespace tc {
 template <bool LAPLACE>
 __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
-  uint8_t* sA = smem_raw;                               // NQT query tiles: H | L
+  uint8_t* sA = smem_raw;                               // NQT query tiles: H | M | L
   uint8_t* sB = smem_raw + A_BYTES;                     // NS data stages
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + A_BYTES + NS * B_STAGE_BYTES);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + K_BAR_OFFSET);
   uint64_t* full = bars;                 // [NS] data stage loaded
-  uint64_t* empty = bars + NS;           // [NS] data stage consumed (MMA + epilogue)
-  uint64_t* tfull = bars + 2 * NS;       // [2] accumulator buffer written
-  uint64_t* tempty = bars + 2 * NS + 2;  // [2] accumulator buffer drained
-  uint64_t* qready = bars + 2 * NS + 4;  // query images loaded
-  uint64_t* qempty = bars + 2 * NS + 5;  // query images no longer read by the MMA
-  uint64_t* drain = bars + 2 * NS + 6;   // all MMAs of this CTA finished (exit path)
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * NS + 7);
-  int64_t n_stage_copies = 0, n_query_copies = 0;   // producer: bulk copies issued
+  uint64_t* empty = bars + NS;           // [NS] data stage consumed (MMAs + epilogue)
+  uint64_t* tfull = bars + 2 * NS;       // [2 buffers][NQT] accumulator written
+  uint64_t* tempty = bars + 2 * NS + 4;  // [2 buffers][NQT] accumulator drained
+  uint64_t* qready = bars + 2 * NS + 8;  // query images loaded
+  uint64_t* qempty = bars + 2 * NS + 9;  // query images no longer read by the MMAs
+  uint64_t* drain = bars + 2 * NS + 10;  // all MMAs of this CTA finished (exit path)
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * NS + 11);
+  uint32_t n_stage_copies = 0, n_query_copies = 0;   // producer: bulk copies issued
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -73,9 +78,9 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], MMA_ISSUERS + EPI_WARPS);
     }
-    for (int b = 0; b < 2; ++b) {
-      mbar_init(&tfull[b], MMA_ISSUERS);
-      mbar_init(&tempty[b], EPI_WARPS);
+    for (int i = 0; i < 2 * NQT; ++i) {
+      mbar_init(&tfull[i], 1);
+      mbar_init(&tempty[i], EPI_WARPS / NQT);
     }
     mbar_init(qready, 1);
     mbar_init(qempty, MMA_ISSUERS);
@@ -96,83 +101,102 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
   const int64_t units = p.q_blocks * p.splits;
   const int64_t u_begin = (int64_t)blockIdx.x * units / gridDim.x;
   const int64_t u_end = (int64_t)(blockIdx.x + 1) * units / gridDim.x;
+  const int64_t qb_begin = u_begin / p.splits;
+  const int64_t sp_begin = u_begin - qb_begin * p.splits;
 
   if (warp == PRODUCER_WARP) {
     if (lane == 0) {
-      int64_t& g = n_stage_copies;
-      int64_t& k = n_query_copies;
+      uint32_t& g = n_stage_copies;
+      uint32_t& k = n_query_copies;
+      int s = 0;
+      uint32_t ph = 0;
+      int64_t qb = qb_begin, sp = sp_begin;
       for (int64_t u = u_begin; u < u_end; ++u) {
-        const int64_t qb = u / p.splits, sp = u % p.splits;
-        if (!mbar_wait(qempty, (uint32_t)((k & 1) ^ 1), 1)) goto done;
+        if (!mbar_wait(qempty, (k & 1u) ^ 1u, 1)) goto done;
         mbar_arrive_expect_tx(qready, A_BYTES);
         bulk_g2s(sA, p.qimg + qb * (int64_t)A_BYTES, A_BYTES, qready);
         ++k;
         const int64_t t0 = sp * p.tiles_per_split;
         const int64_t t1 = imin<int64_t>(p.n_tiles, t0 + p.tiles_per_split);
-        for (int64_t t = t0; t < t1; ++t) {
-          const int s = (int)(g % NS);
-          if (!mbar_wait(&empty[s], (uint32_t)(((g / NS) & 1) ^ 1), 2)) goto done;
-          mbar_arrive_expect_tx(&full[s], B_STAGE_BYTES);
-          bulk_g2s(sB + s * B_STAGE_BYTES, p.ximg + t * (int64_t)B_STAGE_BYTES, B_STAGE_BYTES, &full[s]);
+        const uint8_t* src = p.ximg + t0 * (int64_t)KB_STAGE_BYTES;
+        for (int64_t t = t0; t < t1; ++t, src += KB_STAGE_BYTES) {
+          if (!mbar_wait(&empty[s], ph ^ 1u, 2)) goto done;
+          mbar_arrive_expect_tx(&full[s], KB_STAGE_BYTES);
+          bulk_g2s(sB + s * KB_STAGE_BYTES, src, KB_STAGE_BYTES, &full[s]);
           ++g;
+          if (++s == NS) {
+            s = 0;
+            ph ^= 1u;
+          }
+        }
+        if (++sp == p.splits) {
+          sp = 0;
+          ++qb;
         }
       }
     }
   } else if (warp == MMA_WARP || warp == MMA_WARP2) {
-    // Two issuing threads, two query tiles each: one thread issuing all 28
-    // MMAs of a tile falls behind when it shares its scheduler with busy
-    // epilogue warps.  Each commits its own MMAs; the barriers they signal
-    // count one arrival per issuer.
+    // Two issuing threads, one query tile each, with their own accumulator
+    // barriers: a tile's MMAs wait only for the 8 epilogue warps reading that
+    // tile.  The per-tile path is kept to the waits, the MMAs and the commits
+    // (descriptors of stage s = stage 0 + s * 1 KiB in the 16-byte address
+    // field).
     if (lane == 0) {
-      const uint32_t idesc = idesc_f16_f32(QT, NT);
-      const int a0 = (warp == MMA_WARP) ? 0 : NQT / 2;
-      int64_t g = 0, k = 0;
+      const uint32_t idesc = idesc_f16_f32(QT, KNT);
+      const int a = (warp == MMA_WARP) ? 0 : 1;
+      const uint32_t as = smem_u32(sA + a * A_TILE_BYTES);
+      const uint64_t a_h = smem_desc_kmajor(as, 128, 8 * H_ROW_BYTES);
+      const uint64_t a_m = smem_desc_kmajor(as + A_M_OFFSET, 128, 8 * L_ROW_BYTES);
+      const uint64_t a_l = smem_desc_kmajor(as + A_L_OFFSET, 128, 8 * L_ROW_BYTES);
+      const uint32_t bs0 = smem_u32(sB);
+      const uint64_t b_h0 = smem_desc_kmajor(bs0, 128, 8 * H_ROW_BYTES);
+      const uint64_t b_m0 = smem_desc_kmajor(bs0 + KB_M_OFFSET, 128, 8 * L_ROW_BYTES);
+      const uint64_t b_l0 = smem_desc_kmajor(bs0 + KB_L_OFFSET, 128, 8 * L_ROW_BYTES);
+      const uint32_t d0 = tmem_base + (uint32_t)(a * KNT);
+      uint32_t g = 0, k = 0, ph = 0;
+      int s = 0;
+      int64_t sp = sp_begin;
       for (int64_t u = u_begin; u < u_end; ++u, ++k) {
-        const int64_t sp = u % p.splits;
-        if (!mbar_wait(qready, (uint32_t)(k & 1), 3)) goto done;
+        if (!mbar_wait(qready, k & 1u, 3)) goto done;
         const int64_t t0 = sp * p.tiles_per_split;
-        const int64_t t1 = imin<int64_t>(p.n_tiles, t0 + p.tiles_per_split);
-        for (int64_t t = t0; t < t1; ++t, ++g) {
-          const int s = (int)(g % NS);
-          const int b = (int)(g & 1);
-          if (!mbar_wait(&full[s], (uint32_t)((g / NS) & 1), 4)) goto done;
-          if (!mbar_wait(&tempty[b], (uint32_t)(((g >> 1) & 1) ^ 1), 5)) goto done;
+        const int nt = (int)(imin<int64_t>(p.n_tiles, t0 + p.tiles_per_split) - t0);
+        for (int i = 0; i < nt; ++i, ++g) {
+          const uint32_t b = g & 1u;
+          if (!mbar_wait(&full[s], ph, 4)) goto done;
+          if (!mbar_wait(&tempty[b * NQT + a], ((g >> 1) & 1u) ^ 1u, 5)) goto done;
           tc_fence_after();
-          const uint32_t bs = smem_u32(sB + s * B_STAGE_BYTES);
-          const uint64_t b_h = smem_desc_kmajor(bs, 128, 8 * H_ROW_BYTES);
-          const uint64_t b_m = smem_desc_kmajor(bs + B_M_OFFSET, 128, 8 * L_ROW_BYTES);
-          const uint64_t b_l = smem_desc_kmajor(bs + B_L_OFFSET, 128, 8 * L_ROW_BYTES);
-#pragma unroll
-          for (int a = a0; a < a0 + NQT / 2; ++a) {
-            const uint32_t as = smem_u32(sA + a * A_TILE_BYTES);
-            mma_s_tile<true>(tmem_base + (uint32_t)(b * (NQT * NT) + a * NT), smem_desc_kmajor(as, 128, 8 * H_ROW_BYTES),
-                       smem_desc_kmajor(as + A_M_OFFSET, 128, 8 * L_ROW_BYTES),
-                       smem_desc_kmajor(as + A_L_OFFSET, 128, 8 * L_ROW_BYTES), b_h, b_m, b_l, idesc);
-          }
-          mma_commit(&tfull[b]);
+          const uint64_t so = (uint64_t)(s * (KB_STAGE_BYTES >> 4));
+          mma_s_tile<true>(d0 + b * (uint32_t)(NQT * KNT), a_h, a_m, a_l, b_h0 + so, b_m0 + so, b_l0 + so, idesc);
+          mma_commit(&tfull[b * NQT + a]);
           mma_commit(&empty[s]);
+          if (++s == NS) {
+            s = 0;
+            ph ^= 1u;
+          }
         }
         mma_commit(qempty);
+        if (++sp == p.splits) sp = 0;
       }
     }
   } else {
     // ---------------- epilogue warps ----------------
-    const int qt = warp >> 2;          // query tile within the unit
+    const int qt = warp >> 3;          // query tile within the unit
+    const int half = (warp >> 2) & 1;  // column half of the 128-point data tile
     const int quarter = warp & 3;      // TMEM lane quarter
-    const int row = quarter * 32 + lane;
     const uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
     const float out_mul = p.scales->out_mul;
     const bool scaled = out_mul != 1.0f;
-    int64_t g = 0;
+    uint32_t g = 0;
+    int s = 0;
     int64_t prev_qb = -1;
-    float s_carry = 0.f;   // approximate sum of this query over the splits already done here
+    int64_t qb = qb_begin, sp = sp_begin;
+    float s_carry = 0.f;   // approximate sum of this query's half over the splits already done here
     for (int64_t u = u_begin; u < u_end; ++u) {
-      const int64_t qb = u / p.splits, sp = u % p.splits;
       if (qb != prev_qb) {
         s_carry = 0.f;
         prev_qb = qb;
       }
-      const int64_t gi = qb * (NQT * QT) + qt * QT + row;   // padded query index
+      const int64_t gi = qb * (NQT * QT) + qt * QT + quarter * 32 + lane;   // padded query index
       float qx[FSK_D];
 #pragma unroll
       for (int kk = 0; kk < FSK_D; kk += 4) {
@@ -182,29 +206,38 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
       Comp acc{0.f, 0.f};
       float corr = 0.f;
       const int64_t t0 = sp * p.tiles_per_split;
-      const int64_t t1 = imin<int64_t>(p.n_tiles, t0 + p.tiles_per_split);
-      for (int64_t t = t0; t < t1; ++t, ++g) {
-        const int s = (int)(g % NS);
-        const int b = (int)(g & 1);
-        const int valid = (int)imin<int64_t>(NT, p.n - t * NT);
-        if (!mbar_wait(&tfull[b], (uint32_t)((g >> 1) & 1), 6)) goto done;
+      const int nt = (int)(imin<int64_t>(p.n_tiles, t0 + p.tiles_per_split) - t0);
+      // columns of this thread's half of tile t0 + i: first data index and valid count
+      int64_t col0 = t0 * KNT + half * (KNT / 2);
+      for (int i = 0; i < nt; ++i, ++g, col0 += KNT) {
+        const uint32_t b = g & 1u;
+        const int valid = (int)imin<int64_t>(KNT / 2, p.n - col0);   // may be <= 0
+        // (a timed-out wait ends the whole warp: it must stay converged)
+        if (!__all_sync(0xffffffffu, mbar_wait(&tfull[b * NQT + qt], (g >> 1) & 1u, 6))) goto done;
         tc_fence_after();
-        const uint8_t* stage = sB + s * B_STAGE_BYTES;
+        const uint8_t* xrows = sB + s * KB_STAGE_BYTES + KB_X_OFFSET + half * (KNT / 2) * (FSK_D * 4);
+        float tsum = 0.f;
 #pragma unroll 1
-        for (int c = 0; c < NT / 32; ++c) {
+        for (int c = 0; c < KNT / 64; ++c) {
           uint32_t r[32];
-          tmem_ld32(tmem_base + lane_off + (uint32_t)(b * (NQT * NT) + qt * NT + c * 32), r);
+          tmem_ld32(tmem_base + lane_off + b * (uint32_t)(NQT * KNT) + (uint32_t)(qt * KNT + half * (KNT / 2) + c * 32),
+                    r);
           tmem_ld_wait();
-          if (c == NT / 32 - 1) {
+          if (c == KNT / 64 - 1) {
             // accumulator buffer fully read into registers: release it
             tc_fence_before();
             __syncwarp();
-            if (lane == 0) mbar_arrive(&tempty[b]);
+            if (lane == 0) mbar_arrive(&tempty[b * NQT + qt]);
           }
           float e[32];
           if (scaled) {
 #pragma unroll
-            for (int j = 0; j < 32; ++j) e[j] = __uint_as_float(r[j]) * out_mul;
+            for (int j = 0; j < 32; j += 2) {
+              const float2 v = __fmul2_rn(make_float2(__uint_as_float(r[j]), __uint_as_float(r[j + 1])),
+                                          make_float2(out_mul, out_mul));
+              e[j] = v.x;
+              e[j + 1] = v.y;
+            }
           } else {
 #pragma unroll
             for (int j = 0; j < 32; ++j) e[j] = __uint_as_float(r[j]);
@@ -216,10 +249,11 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
             if (LAPLACE) v *= fmaf(e[j], 0.69314718055994531f, 1.0f + 0.5f * FSK_D);
             e[j] = v;
           }
-          if (valid < NT) {  // ragged last data tile: drop padding columns
+          const int cvalid = valid - c * 32;   // valid columns of this chunk (may be <= 0 or > 32)
+          if (cvalid < 32) {  // ragged last data tile: drop padding columns
 #pragma unroll
             for (int j = 0; j < 32; ++j)
-              if (c * 32 + j >= valid) e[j] = 0.f;
+              if (j >= cvalid) e[j] = 0.f;
           }
           // packed pairwise sum (f32x2 adds on register pairs)
           float2 pa = make_float2(e[0], e[1]), pb = make_float2(e[2], e[3]);
@@ -232,7 +266,8 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
           float cs = pa.x + pa.y;
           // Near-pair test: a chunk holding more than NEAR_FRACTION of the
           // running sum (this chunk included) may contain a dominant term.
-          const bool trig = fabsf(cs) > (s_carry + fabsf(acc.s) + fabsf(cs)) * NEAR_FRACTION;
+          const float run = s_carry + fabsf(acc.s) + fabsf(tsum);
+          const bool trig = fabsf(cs) > (run + fabsf(cs)) * NEAR_FRACTION;
           if (__any_sync(0xffffffffu, trig)) {
             // Triggered lanes replace their chunk's largest term by its exact
             // value.  The argmax rides in the low 5 mantissa bits of each term
@@ -242,7 +277,7 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
             // one pair each, in lock-step.
             if (trig) {
               uint32_t key[32];
-              float2 qa = make_float2(0.f, 0.f), qb = make_float2(0.f, 0.f);
+              float2 qa = make_float2(0.f, 0.f), qc = make_float2(0.f, 0.f);
 #pragma unroll
               for (int j = 0; j < 32; j += 2) {
                 // terms are >= 0 except with the Laplace factor
@@ -251,7 +286,7 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
                 key[j + 1] = (__float_as_uint(a1) & ~31u) | (uint32_t)(j + 1);
                 const float v0 = LAPLACE ? copysignf(__uint_as_float(key[j]), e[j]) : __uint_as_float(key[j]);
                 const float v1 = LAPLACE ? copysignf(__uint_as_float(key[j + 1]), e[j + 1]) : __uint_as_float(key[j + 1]);
-                if (j & 2) qb = __fadd2_rn(qb, make_float2(v0, v1));
+                if (j & 2) qc = __fadd2_rn(qc, make_float2(v0, v1));
                 else qa = __fadd2_rn(qa, make_float2(v0, v1));
               }
               // max tree over the keys
@@ -260,7 +295,7 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
 #pragma unroll
                 for (int j = 0; j < w; ++j) key[j] = max(key[j], key[j + w]);
               const uint32_t kmax = key[0];
-              qa = __fadd2_rn(qa, qb);
+              qa = __fadd2_rn(qa, qc);
               cs = qa.x + qa.y;
               const int j = (int)(kmax & 31u);
               float approx = __uint_as_float(kmax);
@@ -269,24 +304,31 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
                 for (int jj = 0; jj < 32; ++jj)
                   if (jj == j) approx = copysignf(approx, e[jj]);
               }
-              const float dist = exact_dist(stage, c * 32 + j, qx);
+              const float dist = exact_dist(xrows, c * 32 + j, qx, 0);
               float ex = exp2_neg_scaled(dist, p.c2, p.c2_lo);
               if (LAPLACE) ex *= fmaf(-p.c1, dist, 1.0f + 0.5f * FSK_D);
-              if (c * 32 + j >= valid) ex = 0.f;
+              if (j >= cvalid) ex = 0.f;
               corr += ex - approx;
             }
             __syncwarp();
           }
-          acc.add(cs);
+          tsum += cs;
         }
+        acc.add(tsum);
+        // the stage's x rows are no longer read by this warp
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[s]);
+        if (++s == NS) s = 0;
       }
       s_carry += fabsf(acc.s + corr);
       if (gi < p.m) {
         const double v = (double)acc.s + (double)acc.c + (double)corr;
         if (p.atomic_acc) atomicAdd(&p.atomic_acc[gi], v);
-        else p.partials[sp * p.m + gi] = v;
+        else p.partials[(2 * sp + half) * p.m + gi] = v;
+      }
+      if (++sp == p.splits) {
+        sp = 0;
+        ++qb;
       }
     }
   }
@@ -294,9 +336,9 @@ done:
   // Exit path (also after a timed-out wait): let this CTA's bulk copies and
   // MMAs finish before shared and tensor memory are released.
   if (warp == PRODUCER_WARP && lane == 0) {
-    for (int64_t i = imax<int64_t>(0, n_stage_copies - NS); i < n_stage_copies; ++i)
-      mbar_wait(&full[i % NS], (uint32_t)((i / NS) & 1), 7);
-    if (n_query_copies > 0) mbar_wait(qready, (uint32_t)((n_query_copies - 1) & 1), 8);
+    for (uint32_t i = n_stage_copies > (uint32_t)NS ? n_stage_copies - NS : 0u; i < n_stage_copies; ++i)
+      mbar_wait(&full[i % NS], (i / NS) & 1u, 7);
+    if (n_query_copies > 0) mbar_wait(qready, (n_query_copies - 1) & 1u, 8);
   }
   if ((warp == MMA_WARP || warp == MMA_WARP2) && lane == 0) {
     mma_commit(drain);   // one arrival per issuing thread, when its MMAs have finished
@@ -377,7 +419,7 @@ __global__ void scale_select_kernel(TcScales* sc) {
   sc->out_mul = ldexpf(1.f, es);
 }
 
-// data tile image: [H (NT x 32 fp16) | L (NT x 16 fp16) | x (NT x 16 FP32)]
+// data tile image: [H (128 x 32 fp16) | M (128 x 16 fp16) | L (128 x 16 fp16) | x (128 x 16 FP32)]
 __global__ void prep_data_kernel(const float* __restrict__ x, int64_t n, int64_t n_pad,
                                  const float* __restrict__ mu, float c2, const TcScales* __restrict__ sc,
                                  uint8_t* __restrict__ img) {
@@ -393,12 +435,12 @@ __global__ void prep_data_kernel(const float* __restrict__ x, int64_t n, int64_t
     nrm = fmaf(cv, cv, nrm);
     v[k] = ok ? cv * sc->x_scale : 0.f;
   }
-  uint8_t* tile = img + (j / NT) * (int64_t)B_STAGE_BYTES;
-  const int r = (int)(j % NT);
+  uint8_t* tile = img + (j / KNT) * (int64_t)KB_STAGE_BYTES;
+  const int r = (int)(j % KNT);
   const float beta = ok ? -c2 * nrm * sc->b_scale : 0.f;
-  write_operand_row(tile, tile + B_M_OFFSET, tile + B_L_OFFSET, r, v, beta, ok ? ldexpf(1.f, sc->pad[0]) : 0.f,
+  write_operand_row(tile, tile + KB_M_OFFSET, tile + KB_L_OFFSET, r, v, beta, ok ? ldexpf(1.f, sc->pad[0]) : 0.f,
                     true);
-  float4* xr = reinterpret_cast<float4*>(tile + B_X_OFFSET + r * (FSK_D * 4));
+  float4* xr = reinterpret_cast<float4*>(tile + KB_X_OFFSET + r * (FSK_D * 4));
 #pragma unroll
   for (int k = 0; k < 4; ++k) xr[k] = make_float4(xo[4 * k], xo[4 * k + 1], xo[4 * k + 2], xo[4 * k + 3]);
 }
@@ -458,10 +500,11 @@ void plan_splits(TcPlan& pl) {
 TcPlan plan_kde16(int64_t m, int64_t n) {
   TcPlan pl;
   pl.m_pad = (m + NQT * QT - 1) / (NQT * QT) * (NQT * QT);
-  pl.n_tiles = (n + NT - 1) / NT;
-  pl.n_pad = pl.n_tiles * NT;
+  pl.n_tiles = (n + KNT - 1) / KNT;
+  pl.n_pad = pl.n_tiles * KNT;
   pl.q_blocks = pl.m_pad / (NQT * QT);
   plan_splits(pl);
+  pl.part_rows = 2 * pl.splits;   // one row per (split, column half)
   return pl;
 }
 
@@ -470,8 +513,8 @@ size_t tc_kde16_ws_bytes(const TcPlan& pl, int64_t m, bool atomic) {
   b += align_up(sizeof(TcScales), 256);
   b += align_up((size_t)pl.q_blocks * A_BYTES, 256);
   b += align_up((size_t)pl.m_pad * FSK_D * sizeof(float), 256);
-  b += align_up((size_t)pl.n_tiles * B_STAGE_BYTES, 256);
-  b += align_up((size_t)(atomic ? 1 : pl.splits) * m * sizeof(double), 256);
+  b += align_up((size_t)pl.n_tiles * KB_STAGE_BYTES, 256);
+  b += align_up((size_t)(atomic ? 1 : pl.part_rows) * m * sizeof(double), 256);
   return b;
 }
 
@@ -481,8 +524,8 @@ int launch_kde16_tc(const float* q, int64_t m, const float* x, int64_t n, const 
   TcScales* sc = c.take<TcScales>(1);
   uint8_t* qimg = c.take<uint8_t>((size_t)pl.q_blocks * A_BYTES);
   float* qexact = c.take<float>((size_t)pl.m_pad * FSK_D);
-  uint8_t* ximg = c.take<uint8_t>((size_t)pl.n_tiles * B_STAGE_BYTES);
-  double* part = c.take<double>((size_t)(atomic ? 1 : pl.splits) * m);
+  uint8_t* ximg = c.take<uint8_t>((size_t)pl.n_tiles * KB_STAGE_BYTES);
+  double* part = c.take<double>((size_t)(atomic ? 1 : pl.part_rows) * m);
   if (!c.fits()) return FSK_ERR_WORKSPACE_TOO_SMALL;
   *partials_out = part;
 

@@ -600,6 +600,7 @@ TcPlan plan_score16(int64_t n) {
   pl.n_pad = pl.n_tiles * NT;
   pl.q_blocks = pl.m_pad / (SNQT * QT);
   plan_splits(pl);
+  pl.part_rows = 2 * pl.splits;   // pdf rows: one per (split, column half)
   return pl;
 }
 
