@@ -9,37 +9,43 @@
 // allow_tf32), as FP64 partials per data split; the weighted sum is kept
 // centred (sum_j phi_ij (x_j - mu)) and mu * pdf_sum is added back in FP64.
 //
-// How (per 128-query x 64-point tile):
-//  * S = the log2-domain exponent a2 + 15, from the operand images of the KDE
-//    kernel (fsk_tc_kde16.cu), two-part product: four tcgen05.mma;
-//    the +15 rides in the query's bias term, so 2^S = phi * 2^15 and the
-//    weights keep fp16 normal range down to phi ~ 2^-29.
+// How (per 256-query x 64-point tile):
+//  * S = the log2-domain exponent a2 + 15, two-part fp16 product of the
+//    operand images of the KDE kernel (fsk_tc_kde16.cu): four tcgen05.mma
+//    per query tile, the query operand (hi | mid rows) read from tensor
+//    memory, where the epilogue warps copy it at the start of each unit (an
+//    M=128, K=16 MMA with both operands in shared memory costs ~48 cycles,
+//    bound by the operand reads; with A in tensor memory it runs at the
+//    math rate when enough threads issue).  The +15 rides in the query's
+//    bias term, so 2^S = phi * 2^15 and the weights keep fp16 normal range
+//    down to phi ~ 2^-29.
 //  * Epilogue: tcgen05.ld, ex2.approx, pdf chunk sums, the exact near-pair
 //    recompute of the KDE kernel (the recomputed value also replaces the
 //    approximate one in the weights), then the weights are split into fp16
-//    hi + lo and stored to tensor memory with tcgen05.st.
-//  * The weights are written back into the tensor-memory columns their S
-//    came from, as fp16 hi | lo, and
-//    W += (Phi_hi + Phi_lo) [X_hi | X_lo]: tcgen05.mma with the A operand
-//    (weights, M=128 x K=64) read from tensor memory and the B operand
-//    ((x_j - mu) 2^ew as fp16 hi and lo rows, K-major over the data points)
-//    from the data stage, N = 32, FP32 accumulation over a group of S_GROUP
-//    tiles, then added into compensated FP32 sums.
+//    hi + lo and stored with tcgen05.st over the tensor-memory columns their
+//    S came from.
+//  * W += Phi_hi [X_hi | X_lo] + Phi_lo X_hi: tcgen05.mma with the A operand
+//    (weights, M=128 x K=16 per step) read from tensor memory and the B
+//    operand ((x_j - mu) 2^ew as fp16 hi and lo rows, K-major over the data
+//    points) from the data stage, FP32 accumulation over a group of S_GROUP
+//    tiles, then added into compensated FP32 sums.  Four issuing threads,
+//    one per (query tile, weight part), each with its own accumulator: a
+//    single thread issues an M=128, K=16, N=32 MMA every ~46 cycles, four
+//    reach the tensor core's math rate.
 //
-// Pipeline (one persistent CTA per SM, 20 warps):
+// Pipeline (one persistent CTA per SM, 23 warps):
 //   warp 16 : producer (bulk copies of query images per unit, data stages).
-//   warps 17, 19 : issue S for query tiles 0 and 1 (one lane each), up to
+//   warps 17, 18 : issue S for query tiles 0 and 1 (one lane each), up to
 //             NBUF tiles ahead of W; warp 17 owns TMEM.
-//   warp 18 : issues the weighted-sum MMAs (one lane).  An M=128, K=16
-//             tcgen05.mma costs ~46 cycles whatever N <= 64 is, so this
-//             product is the expensive part: two N=32 MMAs per K step, and
-//             the epilogue never waits for it.
+//   warps 19-22 : issue the weighted-sum MMAs of (query tile, weight part)
+//             (0, hi), (0, lo), (1, hi), (1, lo).
 //   warps 0-15: epilogue; warp w: query tile w/8, data-column half (w/4)&1,
 //             TMEM lane quarter w&3.  The two column halves of a row keep
 //             separate pdf partials (written as two virtual splits) and
 //             read disjoint halves of the weighted-sum features.
-// TMEM: S / weights [NBUF buffers][2 query tiles][64]
-//       | W [2 group parities][2 tiles][X_hi part 16 | X_lo part 16].
+// TMEM: A operands [2 query tiles][hi 16 | mid 8 | -]  (columns 0-63)
+//       | S / weights [NBUF buffers][2 query tiles][64]  (64-319)
+//       | W [2 group parities][2 query tiles][hi part 32 | lo part 16]  (320-511).
 #include <cuda_fp16.h>
 
 #include "fsk_kernels.cuh"
@@ -63,14 +69,18 @@ constexpr int S_A_BYTES = SNQT * A_TILE_BYTES;             // 32 KB
 constexpr int S_EPI_WARPS = 8 * SNQT;
 constexpr int S_PRODUCER_WARP = S_EPI_WARPS;
 constexpr int S_MMA_WARP = S_EPI_WARPS + 1;     // issues the S MMAs of query tile 0, owns TMEM
-constexpr int W_MMA_WARP = S_EPI_WARPS + 2;     // issues the weighted-sum MMAs
-constexpr int S_MMA_WARP2 = S_EPI_WARPS + 3;    // issues the S MMAs of query tile 1
-constexpr int S_THREADS = (S_EPI_WARPS + 4) * 32;
+constexpr int S_MMA_WARP2 = S_EPI_WARPS + 2;    // issues the S MMAs of query tile 1
+constexpr int W_MMA_WARP = S_EPI_WARPS + 3;     // first of the W_ISSUERS weighted-sum issuers
+constexpr int W_ISSUERS = 2 * SNQT;             // (query tile, weight part hi / lo)
+constexpr int S_THREADS = (S_EPI_WARPS + 3 + W_ISSUERS) * 32;
 constexpr int S_GROUP = 8;                                 // data tiles per W accumulation
-constexpr int NBUF = 3;                                    // S / weight buffers in TMEM
-constexpr int WN = 2 * FSK_D;                              // W MMA N: X_hi and X_lo rows
-constexpr int T_S = 0;
-constexpr int T_W = NBUF * SNQT * NT;                      // 384
+constexpr int NBUF = 2;                                    // S / weight buffers in TMEM
+constexpr int WN = 2 * FSK_D;                              // W MMA N, hi weights: X_hi and X_lo rows
+constexpr int WN_LO = FSK_D;                               // W MMA N, lo weights: X_hi rows
+constexpr int T_A = 0;                                     // [SNQT][32]: hi 16 | mid 8
+constexpr int T_S = 64;
+constexpr int T_W = T_S + NBUF * SNQT * NT;                // 320
+constexpr int W_TILE_COLS = WN + WN_LO;                    // 48 per (parity, query tile)
 constexpr int S_TMEM_COLS = 512;
 // exact-recompute corrections of the weighted sums: [unit parity][column half][256 rows][16] FP32
 // original coordinates of the unit's 256 queries (exact near-pair recompute)
@@ -91,11 +101,11 @@ constexpr float PHI_LOG2_SCALE = 15.0f;                    // weights are phi * 
 // the tensor core's per-instruction cost), whose exponent error is ~8x the
 // three-part one's, so the near-pair threshold is 1/64 of the running sum.
 constexpr float SCORE_NEAR_FRACTION = 1.0f / 64.0f;
-static_assert(T_W + 2 * SNQT * WN <= S_TMEM_COLS, "TMEM budget");
+static_assert(T_W + 2 * SNQT * W_TILE_COLS <= S_TMEM_COLS, "TMEM budget");
 static_assert(S_XTL_OFFSET == S_XTH_OFFSET + 16 * XT_ROW_BYTES, "X_lo rows follow X_hi rows (one N=32 operand)");
 static_assert(S_STAGE_BYTES % 16 == 0 && S_A_BYTES % 16 == 0 && S_QX_BYTES % 16 == 0, "bulk copy granularity");
 static_assert(S_SMEM_BYTES <= 227 * 1024, "shared memory");
-static_assert((2 * SNS + 6 + NBUF * SNQT + 8) * 8 + 4 <= 512, "barrier area");
+static_assert((2 * SNS + 3 * NBUF * SNQT + 4 * SNQT + SNQT + 4) * 8 + 4 <= 512, "barrier area");
 
 struct ScParams {
   const uint8_t* qimg;
@@ -151,20 +161,21 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
   uint8_t* sB = smem_raw + S_B_OFFSET;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + S_BAR_OFFSET);
   float* sMu = reinterpret_cast<float*>(smem_raw + S_MU_OFFSET);
-  uint64_t* full = bars;                      // [SNS] stage loaded
-  uint64_t* empty = bars + SNS;               // [SNS] stage consumed (W MMA + epilogue)
-  uint64_t* tfull = bars + 2 * SNS;           // [NBUF] S buffer written
-  // [NBUF][SNQT] weights of a query tile stored in a buffer.  One barrier per
-  // buffer: the epilogue may run NBUF tiles ahead of the W MMA, and a
+  uint64_t* full = bars;                          // [SNS] stage loaded
+  uint64_t* empty = bars + SNS;                   // [SNS] stage consumed (W MMAs + epilogue)
+  uint64_t* tfull = bars + 2 * SNS;               // [NBUF][SNQT] S written
+  // [NBUF][SNQT] weights stored.  One barrier per buffer and query tile: a
   // buffer's barrier cannot complete again before its weights are consumed.
-  uint64_t* pready = bars + 2 * SNS + 6;
-  uint64_t* wfull = bars + 2 * SNS + 6 + NBUF * SNQT;        // [2] W group accumulated
-  uint64_t* wempty = wfull + 2;                               // [2] W group read
-  uint64_t* qready = wfull + 4;
-  uint64_t* qempty = wfull + 5;
-  uint64_t* drain = wfull + 6;                // all MMAs of this CTA finished (exit path)
-  uint64_t* cready = wfull + 7;               // unit's W corrections written (epilogue warps)
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(wfull + 8);
+  uint64_t* pready = tfull + NBUF * SNQT;
+  uint64_t* sfree = pready + NBUF * SNQT;         // [NBUF][SNQT] weights read by both W parts
+  uint64_t* wfull = sfree + NBUF * SNQT;          // [2 parities][SNQT] W group accumulated
+  uint64_t* wempty = wfull + 2 * SNQT;            // [2 parities][SNQT] W group read
+  uint64_t* aready = wempty + 2 * SNQT;           // [SNQT] unit's A operand in TMEM
+  uint64_t* qready = aready + SNQT;
+  uint64_t* qempty = qready + 1;
+  uint64_t* drain = qready + 2;                   // all MMAs of this CTA finished (exit path)
+  uint64_t* cready = qready + 3;                  // unit's W corrections written (epilogue warps)
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(qready + 4);
   float* wcorr = reinterpret_cast<float*>(smem_raw + S_WCORR_OFFSET);
   float4* wacc = reinterpret_cast<float4*>(smem_raw + S_WACC_OFFSET);
   int64_t n_stage_copies = 0, n_query_copies = 0;   // producer: bulk copies issued
@@ -175,17 +186,21 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
   if (threadIdx.x == 0) {
     for (int s = 0; s < SNS; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1 + S_EPI_WARPS);   // the W thread's commit + every epilogue warp
+      mbar_init(&empty[s], W_ISSUERS + S_EPI_WARPS);   // the W threads' commits + every epilogue warp
     }
-    for (int b = 0; b < NBUF; ++b) mbar_init(&tfull[b], 2);   // one commit per S thread
-    for (int b = 0; b < 2; ++b) {
-      mbar_init(&wfull[b], 1);
-      mbar_init(&wempty[b], S_EPI_WARPS);
+    for (int i = 0; i < NBUF * SNQT; ++i) {
+      mbar_init(&tfull[i], 1);
+      mbar_init(&pready[i], 8);
+      mbar_init(&sfree[i], 2);
     }
-    for (int i = 0; i < NBUF * SNQT; ++i) mbar_init(&pready[i], 8);
+    for (int i = 0; i < 2 * SNQT; ++i) {
+      mbar_init(&wfull[i], 2);
+      mbar_init(&wempty[i], 8);
+    }
+    for (int a = 0; a < SNQT; ++a) mbar_init(&aready[a], 8);
     mbar_init(qready, 1);
-    mbar_init(qempty, 2 + S_EPI_WARPS);   // last S MMAs of the unit (both S threads) + every epilogue warp
-    mbar_init(drain, 3);
+    mbar_init(qempty, S_EPI_WARPS);
+    mbar_init(drain, 2 + W_ISSUERS);
     mbar_init(cready, S_EPI_WARPS);
     fence_barrier_init();
   }
@@ -225,55 +240,51 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
       }
     }
   } else if (warp == S_MMA_WARP || warp == S_MMA_WARP2) {
-    // S(g) for every tile, up to NBUF tiles ahead of the W MMAs: buffer
-    // g % NBUF is reused once W(g - NBUF) has read its weights, which the
-    // stage barrier of tile g - NBUF signals (it completes with the W
-    // thread's commit; that tile's epilogue arrivals came earlier).  S and W
-    // are issued by different threads because tcgen05.commit tracks every
-    // earlier MMA of its thread: waiting for W(g - NBUF) from one issuing
-    // thread would also wait for the S MMAs issued after it and drain the
-    // tensor pipe every tile.
-    // Two S threads, one query tile each (one thread issuing all 14 S MMAs of
-    // a tile falls behind when it shares its scheduler with busy warps).
+    // S(g) of one query tile for every tile, up to NBUF tiles ahead of W:
+    // buffer g % NBUF is reused once both W parts of tile g - NBUF have read
+    // its weights (sfree).  S and W are issued by different threads because
+    // tcgen05.commit tracks every earlier MMA of its thread.
     if (lane == 0) {
-      const int a_mine = warp == S_MMA_WARP ? 0 : 1;
+      const int a = warp == S_MMA_WARP ? 0 : 1;
       const uint32_t idesc_s = idesc_f16_f32(QT, NT);
+      const uint32_t a_h = tmem_base + (uint32_t)(T_A + a * 32);   // hi: features | bias; mid at +16
       // descriptors are advanced by adding (bytes >> 4) to the start-address
       // field (shared addresses stay below 2^18 B, so the field cannot carry)
-      const uint32_t as = smem_u32(sA + a_mine * A_TILE_BYTES);
-      const uint64_t a_h = smem_desc_kmajor(as, 128, 8 * H_ROW_BYTES);
-      const uint64_t a_m = smem_desc_kmajor(as + A_M_OFFSET, 128, 8 * L_ROW_BYTES);
-      const uint64_t a_l = smem_desc_kmajor(as + A_L_OFFSET, 128, 8 * L_ROW_BYTES);
       const uint32_t b0 = smem_u32(sB);
       const uint64_t dh0 = smem_desc_kmajor(b0, 128, 8 * H_ROW_BYTES);
       const uint64_t dm0 = smem_desc_kmajor(b0 + B_M_OFFSET, 128, 8 * L_ROW_BYTES);
-      const uint64_t dl0 = smem_desc_kmajor(b0 + B_L_OFFSET, 128, 8 * L_ROW_BYTES);
       TileCursor cs;
       cs.start((int)u_begin, (int)u_end, (int)p.splits, (int)p.tiles_per_split, (int)p.n_tiles);
-      int gs = 0, kq = 0;
+      int gs = 0, ku = 0;
       while (!cs.done()) {
         const int s = gs % SNS;
-        if (cs.t == cs.t0) {   // first tile of a unit: its query images
-          if (!mbar_wait(qready, (uint32_t)(kq & 1), 23)) goto done;
-          ++kq;
+        const int b = gs % NBUF;
+        if (cs.t == cs.t0) {   // first tile of a unit: its A operand in TMEM
+          if (!mbar_wait(&aready[a], (uint32_t)(ku & 1), 23)) goto done;
+          ++ku;
         }
-        const int gp = gs - NBUF;
-        if (gp >= 0 && !mbar_wait(&empty[gp % SNS], (uint32_t)((gp / SNS) & 1), 25)) goto done;
+        if (gs >= NBUF && !mbar_wait(&sfree[b * SNQT + a], (uint32_t)(((gs / NBUF) - 1) & 1), 25)) goto done;
         if (!mbar_wait(&full[s], (uint32_t)((gs / SNS) & 1), 24)) goto done;
         tc_fence_after();
         const uint64_t so = (uint64_t)((s * S_STAGE_BYTES) >> 4);
-        const uint32_t d0 = tmem_base + (uint32_t)(T_S + (gs % NBUF) * (SNQT * NT));
-        mma_s_tile<false>(d0 + (uint32_t)(a_mine * NT), a_h, a_m, a_l, dh0 + so, dm0 + so, dl0 + so, idesc_s);
-        mma_commit(&tfull[gs % NBUF]);
-        if (cs.t == cs.t1 - 1) mma_commit(qempty);   // last S read of this unit's query images
+        const uint32_t d = tmem_base + (uint32_t)(T_S + b * (SNQT * NT) + a * NT);
+        const uint64_t b_h = dh0 + so;
+        mma_f16_ts(d, a_h, dm0 + so, idesc_s, 0u);                     // hi . mid
+        mma_f16_ts(d, a_h + 16u, b_h, idesc_s, 1u);                    // mid . hi
+        mma_f16_ts(d, a_h, b_h, idesc_s, 1u);                          // hi . hi
+        mma_f16_ts(d, a_h + 8u, b_h + (uint64_t)(256 >> 4), idesc_s, 1u);   // bias . bias
+        mma_commit(&tfull[b * SNQT + a]);
         ++gs;
         cs.next();
       }
     }
-  } else if (warp == W_MMA_WARP) {
-    // W(g) once the epilogue has stored tile g's weights (both query tiles).
+  } else if (warp >= W_MMA_WARP) {
+    // W(g) of one (query tile, weight part) once the epilogue warps of that
+    // query tile have stored tile g's weights.
     if (lane == 0) {
-      const uint32_t idesc_w = idesc_f16_f32(QT, WN);
+      const int wi = warp - W_MMA_WARP;
+      const int a = wi >> 1, part = wi & 1;   // part 0: hi weights x [X_hi | X_lo]; 1: lo weights x X_hi
+      const uint32_t idesc_w = idesc_f16_f32(QT, part ? WN_LO : WN);
       const uint64_t dx0 = smem_desc_kmajor(smem_u32(sB) + S_XTH_OFFSET, 128, 8 * XT_ROW_BYTES);
       TileCursor cw;
       cw.start((int)u_begin, (int)u_end, (int)p.splits, (int)p.tiles_per_split, (int)p.n_tiles);
@@ -285,28 +296,22 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
         const bool first = pos == 0;
         const bool last = pos == S_GROUP - 1 || cw.t == cw.t1 - 1;
         const int par = grp & 1;
-        if (first && !mbar_wait(&wempty[par], (uint32_t)(((grp >> 1) & 1) ^ 1), 26)) goto done;
-#pragma unroll
-        for (int a = 0; a < SNQT; ++a)
-          if (!mbar_wait(&pready[b * SNQT + a], (uint32_t)((gw / NBUF) & 1), 27)) goto done;
+        if (first && !mbar_wait(&wempty[par * SNQT + a], (uint32_t)(((grp >> 1) & 1) ^ 1), 26)) goto done;
+        if (!mbar_wait(&pready[b * SNQT + a], (uint32_t)((gw / NBUF) & 1), 27)) goto done;
         tc_fence_after();
         const uint64_t xd0 = dx0 + (uint64_t)((s * S_STAGE_BYTES) >> 4);
-        const uint32_t ph0 = tmem_base + (uint32_t)(T_S + b * (SNQT * NT));
-        const uint32_t d0 = tmem_base + (uint32_t)(T_W + par * (SNQT * WN));
+        const uint32_t ph = tmem_base + (uint32_t)(T_S + b * (SNQT * NT) + a * NT + part * 16);
+        const uint32_t d = tmem_base + (uint32_t)(T_W + par * (SNQT * W_TILE_COLS) + a * W_TILE_COLS + part * WN);
 #pragma unroll
-        for (int a = 0; a < SNQT; ++a) {
-#pragma unroll
-          for (int ks = 0; ks < NT / 16; ++ks) {
-            // data columns 16 ks .. +15: column half ks/2, weights hi at +0, lo at +16
-            const uint32_t wa = ph0 + (uint32_t)(a * NT + 32 * (ks >> 1) + 8 * (ks & 1));
-            const uint64_t xd = xd0 + (uint64_t)(ks * (256 >> 4));
-            mma_f16_ts(d0 + (uint32_t)(a * WN), wa, xd, idesc_w, (first && ks == 0) ? 0u : 1u);
-            mma_f16_ts(d0 + (uint32_t)(a * WN), wa + 16, xd, idesc_w, 1u);
-          }
+        for (int ks = 0; ks < NT / 16; ++ks) {
+          // data columns 16 ks .. +15: column half ks/2; weights hi at +0, lo at +16
+          const uint32_t wa = ph + (uint32_t)(32 * (ks >> 1) + 8 * (ks & 1));
+          mma_f16_ts(d, wa, xd0 + (uint64_t)(ks * (256 >> 4)), idesc_w, (first && ks == 0) ? 0u : 1u);
         }
+        mma_commit(&sfree[b * SNQT + a]);
         mma_commit(&empty[s]);
         if (last) {
-          mma_commit(&wfull[par]);
+          mma_commit(&wfull[par * SNQT + a]);
           ++grp;
         }
         ++gw;
@@ -348,6 +353,35 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
       const int gi = qb * (SNQT * QT) + qt * QT + row;
       const int diag_col = qb * (SNQT * QT) + qt * QT + quarter * 32;   // this warp's rows
       float* wc = wcorr + (k_unit & 1) * WC_PAR + half * WC_HALF + wc_row;
+      // The unit's query images: this row's A operand to TMEM (column half 0
+      // copies the hi row, half 1 the mid row).  The S MMAs of the previous
+      // unit have all completed: this warp consumed their accumulators.
+      if (!__all_sync(0xffffffffu, mbar_wait(qready, (uint32_t)(k_unit & 1), 36))) goto done;
+      {
+        const uint8_t* tile = sA + qt * A_TILE_BYTES;
+        const uint32_t ta = tmem_base + lane_off + (uint32_t)(T_A + qt * 32);
+        if (half == 0) {
+          uint32_t w[16];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const uint4 v = *reinterpret_cast<const uint4*>(tile + cm_offset(row, 8 * c, H_ROW_BYTES));
+            w[4 * c] = v.x; w[4 * c + 1] = v.y; w[4 * c + 2] = v.z; w[4 * c + 3] = v.w;
+          }
+          tmem_st16(ta, w);
+        } else {
+          uint32_t w[8];
+#pragma unroll
+          for (int c = 0; c < 2; ++c) {
+            const uint4 v = *reinterpret_cast<const uint4*>(tile + A_M_OFFSET + cm_offset(row, 8 * c, L_ROW_BYTES));
+            w[4 * c] = v.x; w[4 * c + 1] = v.y; w[4 * c + 2] = v.z; w[4 * c + 3] = v.w;
+          }
+          tmem_st8(ta + 16u, w);
+        }
+        tmem_st_wait();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&aready[qt]);
+      }
       Comp acc{0.f, 0.f};
       float corr = 0.f;
       constexpr int EPI_T = S_EPI_WARPS * 32;
@@ -360,7 +394,7 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
         const int s = g % SNS;
         const int b = g % NBUF;
         const int valid = (int)imin<int64_t>(NT, p.n - (int64_t)t * NT);
-        if (!mbar_wait(&tfull[b], (uint32_t)((g / NBUF) & 1), 28)) goto done;
+        if (!__all_sync(0xffffffffu, mbar_wait(&tfull[b * SNQT + qt], (uint32_t)((g / NBUF) & 1), 28))) goto done;
         tc_fence_after();
         const uint8_t* stage = sB + s * S_STAGE_BYTES;
         // this warp's 32 S columns; its weights go back into the same columns
@@ -418,8 +452,7 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
             const int j = (int)(kmax & 31u);
             const int col = half * 32 + j;
             const float4* xr = reinterpret_cast<const float4*>(stage + S_X_OFFSET + col * (FSK_D * 4));
-            // exact squared distance, four features at a time (query from
-            // its original coordinates, L1-resident after first use)
+            // exact squared distance, four features at a time
             const float4* qr = reinterpret_cast<const float4*>(sQ + (qt * QT + row) * FSK_D);
             float d0 = 0.f, d1 = 0.f, d2 = 0.f, d3 = 0.f;
 #pragma unroll
@@ -452,12 +485,16 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
         }
         acc.add(cs);
         // fp16 hi / lo weights for the W product, written over this warp's
-        // S columns (hi: 16 columns of packed pairs, then lo)
-        uint32_t hi[16], lo[16];
+        // S columns (hi: 16 columns of packed pairs, then lo), eight pairs at
+        // a time to keep the register peak low
 #pragma unroll
-        for (int j = 0; j < 16; ++j) split_pack(e[2 * j], e[2 * j + 1], hi[j], lo[j]);
-        tmem_st16(my_cols, hi);
-        tmem_st16(my_cols + 16, lo);
+        for (int h8 = 0; h8 < 2; ++h8) {
+          uint32_t hi[8], lo[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) split_pack(e[16 * h8 + 2 * j], e[16 * h8 + 2 * j + 1], hi[j], lo[j]);
+          tmem_st8(my_cols + (uint32_t)(8 * h8), hi);
+          tmem_st8(my_cols + (uint32_t)(16 + 8 * h8), lo);
+        }
         tmem_st_wait();
         tc_fence_before();
         __syncwarp();
@@ -473,18 +510,21 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
           const bool do_read = pass == 0 ? pend : (last && t == t1 - 1);
           if (!do_read) continue;
           const int par = grp & 1;
-          if (!mbar_wait(&wfull[par], (uint32_t)((grp >> 1) & 1), 30)) goto done;
+          if (!__all_sync(0xffffffffu, mbar_wait(&wfull[par * SNQT + qt], (uint32_t)((grp >> 1) & 1), 30))) goto done;
           tc_fence_after();
-          uint32_t wv[8], wl[8];   // X_hi and X_lo parts of this warp's 8 features
-          const uint32_t wcol = tmem_base + lane_off + (uint32_t)(T_W + par * (SNQT * WN) + qt * WN + half * 8);
+          // this warp's 8 features: hi weights x X_hi, hi weights x X_lo, lo weights x X_hi
+          uint32_t wv[8], wl[8], wm[8];
+          const uint32_t wcol = tmem_base + lane_off + (uint32_t)(T_W + par * (SNQT * W_TILE_COLS) + qt * W_TILE_COLS + half * 8);
           tmem_ld8(wcol, wv);
           tmem_ld8(wcol + FSK_D, wl);
+          tmem_ld8(wcol + WN, wm);
           tmem_ld_wait();
 #pragma unroll
-          for (int k = 0; k < 8; ++k) wv[k] = __float_as_uint(__uint_as_float(wv[k]) + __uint_as_float(wl[k]));
+          for (int k = 0; k < 8; ++k)
+            wv[k] = __float_as_uint(__uint_as_float(wv[k]) + (__uint_as_float(wl[k]) + __uint_as_float(wm[k])));
           tc_fence_before();
           __syncwarp();
-          if (lane == 0) mbar_arrive(&wempty[par]);
+          if (lane == 0) mbar_arrive(&wempty[par * SNQT + qt]);
           {
             float4 s0 = wacc[threadIdx.x], s1 = wacc[EPI_T + threadIdx.x];
             float4 e0 = wacc[2 * EPI_T + threadIdx.x], e1 = wacc[3 * EPI_T + threadIdx.x];
@@ -513,9 +553,9 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
       __syncwarp();
       if (lane == 0) {
         mbar_arrive(cready);
-        mbar_arrive(qempty);   // done with this unit's query rows in shared memory
+        mbar_arrive(qempty);   // done with this unit's query images and rows in shared memory
       }
-      if (!mbar_wait(cready, (uint32_t)(k_unit & 1), 35)) goto done;
+      if (!__all_sync(0xffffffffu, mbar_wait(cready, (uint32_t)(k_unit & 1), 35))) goto done;
       {
         float* wc_next = wcorr + ((k_unit + 1) & 1) * WC_PAR + half * WC_HALF + wc_row;
 #pragma unroll
@@ -548,7 +588,7 @@ done:
       mbar_wait(&full[i % SNS], (uint32_t)((i / SNS) & 1), 32);
     if (n_query_copies > 0) mbar_wait(qready, (uint32_t)((n_query_copies - 1) & 1), 33);
   }
-  if ((warp == S_MMA_WARP || warp == S_MMA_WARP2 || warp == W_MMA_WARP) && lane == 0) {
+  if ((warp == S_MMA_WARP || warp == S_MMA_WARP2 || warp >= W_MMA_WARP) && lane == 0) {
     mma_commit(drain);   // one arrival per issuing thread, when its MMAs have finished
     mbar_wait(drain, 0, 34);
   }
