@@ -10,9 +10,9 @@
 // centred (sum_j phi_ij (x_j - mu)) and mu * pdf_sum is added back in FP64.
 //
 // How (per 256-query x 64-point tile):
-//  * S = the log2-domain exponent a2 + 15, two-part fp16 product of the
-//    operand images of the KDE kernel (fsk_tc_kde16.cu): four tcgen05.mma
-//    per query tile, the query operand (hi | mid rows) read from tensor
+//  * S = the log2-domain exponent a2 + 15, three-part fp16 product of the
+//    operand images of the KDE kernel (fsk_tc_kde16.cu): seven tcgen05.mma
+//    per query tile, the query operand (hi | mid | lo rows) read from tensor
 //    memory, where the epilogue warps copy it at the start of each unit (an
 //    M=128, K=16 MMA with both operands in shared memory costs ~48 cycles,
 //    bound by the operand reads; with A in tensor memory it runs at the
@@ -43,7 +43,7 @@
 //             TMEM lane quarter w&3.  The two column halves of a row keep
 //             separate pdf partials (written as two virtual splits) and
 //             read disjoint halves of the weighted-sum features.
-// TMEM: A operands [2 query tiles][hi 16 | mid 8 | -]  (columns 0-63)
+// TMEM: A operands [2 query tiles][hi 16 | mid 8 | lo 8]  (columns 0-63)
 //       | S / weights [NBUF buffers][2 query tiles][64]  (64-319)
 //       | W [2 group parities][2 query tiles][hi part 32 | lo part 16]  (320-511).
 #include <cuda_fp16.h>
@@ -77,7 +77,7 @@ constexpr int S_GROUP = 8;                                 // data tiles per W a
 constexpr int NBUF = 2;                                    // S / weight buffers in TMEM
 constexpr int WN = 2 * FSK_D;                              // W MMA N, hi weights: X_hi and X_lo rows
 constexpr int WN_LO = FSK_D;                               // W MMA N, lo weights: X_hi rows
-constexpr int T_A = 0;                                     // [SNQT][32]: hi 16 | mid 8
+constexpr int T_A = 0;                                     // [SNQT][32]: hi 16 | mid 8 | lo 8
 constexpr int T_S = 64;
 constexpr int T_W = T_S + NBUF * SNQT * NT;                // 320
 constexpr int W_TILE_COLS = WN + WN_LO;                    // 48 per (parity, query tile)
@@ -97,10 +97,9 @@ constexpr int S_WACC_BYTES = 4 * S_EPI_WARPS * 32 * 16;                // 32 KB
 constexpr int S_MU_OFFSET = S_WACC_OFFSET + S_WACC_BYTES;             // data mean, 16 FP32
 constexpr int S_SMEM_BYTES = S_MU_OFFSET + FSK_D * 4;
 constexpr float PHI_LOG2_SCALE = 15.0f;                    // weights are phi * 2^15
-// The S product here is the two-part one (four MMAs: this kernel is bound by
-// the tensor core's per-instruction cost), whose exponent error is ~8x the
-// three-part one's, so the near-pair threshold is 1/64 of the running sum.
-constexpr float SCORE_NEAR_FRACTION = 1.0f / 64.0f;
+// Three-part S product as in the KDE kernel, so the same near-pair threshold
+// (1/8 of the running sum, the excluded self pair's weight included).
+constexpr float SCORE_NEAR_FRACTION = NEAR_FRACTION;
 static_assert(T_W + 2 * SNQT * W_TILE_COLS <= S_TMEM_COLS, "TMEM budget");
 static_assert(S_XTL_OFFSET == S_XTH_OFFSET + 16 * XT_ROW_BYTES, "X_lo rows follow X_hi rows (one N=32 operand)");
 static_assert(S_STAGE_BYTES % 16 == 0 && S_A_BYTES % 16 == 0 && S_QX_BYTES % 16 == 0, "bulk copy granularity");
@@ -247,12 +246,13 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
     if (lane == 0) {
       const int a = warp == S_MMA_WARP ? 0 : 1;
       const uint32_t idesc_s = idesc_f16_f32(QT, NT);
-      const uint32_t a_h = tmem_base + (uint32_t)(T_A + a * 32);   // hi: features | bias; mid at +16
+      const uint32_t a_h = tmem_base + (uint32_t)(T_A + a * 32);   // hi: features | bias; mid at +16, lo at +24
       // descriptors are advanced by adding (bytes >> 4) to the start-address
       // field (shared addresses stay below 2^18 B, so the field cannot carry)
       const uint32_t b0 = smem_u32(sB);
       const uint64_t dh0 = smem_desc_kmajor(b0, 128, 8 * H_ROW_BYTES);
       const uint64_t dm0 = smem_desc_kmajor(b0 + B_M_OFFSET, 128, 8 * L_ROW_BYTES);
+      const uint64_t dl0 = smem_desc_kmajor(b0 + B_L_OFFSET, 128, 8 * L_ROW_BYTES);
       TileCursor cs;
       cs.start((int)u_begin, (int)u_end, (int)p.splits, (int)p.tiles_per_split, (int)p.n_tiles);
       int gs = 0, ku = 0;
@@ -269,7 +269,12 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
         const uint64_t so = (uint64_t)((s * S_STAGE_BYTES) >> 4);
         const uint32_t d = tmem_base + (uint32_t)(T_S + b * (SNQT * NT) + a * NT);
         const uint64_t b_h = dh0 + so;
-        mma_f16_ts(d, a_h, dm0 + so, idesc_s, 0u);                     // hi . mid
+        // three-part product, small terms first (the order of mma_s_tile<true>)
+        const uint64_t b_m = dm0 + so, b_l = dl0 + so;
+        mma_f16_ts(d, a_h + 16u, b_m, idesc_s, 0u);                    // mid . mid
+        mma_f16_ts(d, a_h, b_l, idesc_s, 1u);                          // hi . lo
+        mma_f16_ts(d, a_h + 24u, b_h, idesc_s, 1u);                    // lo . hi
+        mma_f16_ts(d, a_h, b_m, idesc_s, 1u);                          // hi . mid
         mma_f16_ts(d, a_h + 16u, b_h, idesc_s, 1u);                    // mid . hi
         mma_f16_ts(d, a_h, b_h, idesc_s, 1u);                          // hi . hi
         mma_f16_ts(d, a_h + 8u, b_h + (uint64_t)(256 >> 4), idesc_s, 1u);   // bias . bias
@@ -354,7 +359,7 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
       const int diag_col = qb * (SNQT * QT) + qt * QT + quarter * 32;   // this warp's rows
       float* wc = wcorr + (k_unit & 1) * WC_PAR + half * WC_HALF + wc_row;
       // The unit's query images: this row's A operand to TMEM (column half 0
-      // copies the hi row, half 1 the mid row).  The S MMAs of the previous
+      // copies the hi row, half 1 the mid and lo rows).  The S MMAs of the previous
       // unit have all completed: this warp consumed their accumulators.
       if (!__all_sync(0xffffffffu, mbar_wait(qready, (uint32_t)(k_unit & 1), 36))) goto done;
       {
@@ -369,13 +374,14 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
           }
           tmem_st16(ta, w);
         } else {
-          uint32_t w[8];
+          uint32_t w[16];   // mid row, then lo row
 #pragma unroll
-          for (int c = 0; c < 2; ++c) {
-            const uint4 v = *reinterpret_cast<const uint4*>(tile + A_M_OFFSET + cm_offset(row, 8 * c, L_ROW_BYTES));
+          for (int c = 0; c < 4; ++c) {
+            const uint4 v = *reinterpret_cast<const uint4*>(tile + (c < 2 ? A_M_OFFSET : A_L_OFFSET) +
+                                                            cm_offset(row, 8 * (c & 1), L_ROW_BYTES));
             w[4 * c] = v.x; w[4 * c + 1] = v.y; w[4 * c + 2] = v.z; w[4 * c + 3] = v.w;
           }
-          tmem_st8(ta + 16u, w);
+          tmem_st16(ta + 16u, w);
         }
         tmem_st_wait();
         tc_fence_before();
