@@ -98,7 +98,7 @@ def workload_config() -> dict:
         "bandwidth": "silverman",
         "pairs_per_step": N_TRAIN * N_TRAIN + N_TRAIN * N_QUERY,
         "l2": "flushed before each timed step (256 MiB write)",
-        "precision_mode": "fast_tf32 (bf16x3 tensor-core distances + exact FP32 near-pair recompute)",
+        "precision_mode": "fast_tf32 (three-part fp16 tensor-core exponents + exact FP32 near-pair recompute)",
     }
 
 

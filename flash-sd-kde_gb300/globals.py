@@ -5,7 +5,7 @@ Same names and values as the Flash-SD-KDE project's top-level globals.py
 """
 
 # precision modes
-PRECISION_FAST_TF32 = "fast_tf32"      # here: bf16x3 tensor cores + exact near-pair recompute
+PRECISION_FAST_TF32 = "fast_tf32"      # here: three-part fp16 tensor-core exponents + exact near-pair recompute
 PRECISION_FP32_IEEE = "fp32_ieee"      # here: FP32 direct differences on the CUDA cores
 
 # KDE evaluation backends
