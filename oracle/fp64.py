@@ -78,6 +78,26 @@ def empirical_score(data, bandwidth: float, *, eps: float = 1e-12, chunk: int = 
     return pdf, w, score
 
 
+def empirical_score_rows(data, rows, bandwidth: float, *, chunk: int = 1 << 20):
+    """FP64 (pdf_sum, weighted_sum) of reference.py:263-284 for the selected
+    rows only (self pair included), against all n data points: the checker
+    for sizes whose full n^2 oracle would not finish."""
+    x = np.asarray(data, dtype=np.float64)
+    r = np.asarray(rows, dtype=np.int64)
+    inv2h2 = 1.0 / (2.0 * bandwidth * bandwidth)
+    pdf = np.zeros(r.size)
+    w = np.zeros((r.size, x.shape[1]))
+    for i, row in enumerate(r):
+        q = x[row]
+        for s in range(0, x.shape[0], chunk):
+            xb = x[s:s + chunk]
+            dist = ((xb - q) ** 2).sum(axis=1)
+            phi = np.exp(-dist * inv2h2)
+            pdf[i] += phi.sum()
+            w[i] += phi @ xb
+    return pdf, w
+
+
 def debias(data, bandwidth: float, *, eps: float = 1e-12) -> np.ndarray:
     _, _, score = empirical_score(data, bandwidth, eps=eps)
     return np.asarray(data, dtype=np.float64) + 0.5 * bandwidth * bandwidth * score

@@ -1,0 +1,94 @@
+"""Parity at the full sizes of the precision-stress and large configurations
+(n = m = 2^20 offset Student-t; n = 2^22 score; 1-D 2^22 x 2^20), where the
+full FP64 oracle would not finish: size-independent checks (run-to-run
+bitwise determinism, finiteness) plus the FP64 oracle on fixed row / query
+subsets.
+
+Tolerances: relative log-density error vs FP64 1e-6 (spec bar 1e-5);
+pdf_sum 1e-5 relative; weighted_sum 1e-5 relative with an absolute floor of
+1e-5 * max|weighted| (signed sums cancel); 1-D densities 1e-5 relative.
+"""
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_err
+from oracle import fp64
+from oracle import reference_numpy as R
+
+pytestmark = pytest.mark.gpu
+
+
+def test_precision_stress_2p20_offset_student_t(cuda_dev):
+    """n = m = 2^20 heavy-tailed data at a +100 offset, h in {0.5, 1, 2} x
+    Silverman, both precision modes; FP64 log densities on 128 fixed queries."""
+    from fsk import ops, workloads
+
+    n = 1 << 20
+    x_np = workloads.student_t_16d(n, seed=4)
+    q_np = workloads.student_t_16d(n, seed=5)
+    x = torch.from_numpy(x_np).to(cuda_dev)
+    q = torch.from_numpy(q_np).to(cuda_dev)
+    h0 = R.silverman_bandwidth_nd(x_np[:65536])
+    sub = np.random.default_rng(0).choice(n, 128, replace=False)
+    for f in (0.5, 1.0, 2.0):
+        h = h0 * f
+        norm = 1.0 / ((2 * np.pi) ** 8 * h ** 16 * n)
+        ref = fp64.log_density(x_np, q_np[sub], h, q_chunk=128, s_chunk=1 << 15)
+        ok = np.isfinite(ref) & (ref > -80.0)   # densities representable in FP32
+        assert ok.sum() > 32
+        for precision in ("tensor", "ieee"):
+            lp = ops.kde16_sum(q, x, h, precision=precision, out_scale=norm, log_eps=0.0)
+            ops.device_status(cuda_dev)
+            lp = lp.cpu().numpy().astype(np.float64)
+            assert np.isfinite(lp[np.isfinite(lp)]).all()
+            got = lp[sub]
+            rel = np.abs(got[ok] - ref[ok]) / np.abs(ref[ok])
+            assert rel.max() < 1e-6, (f, precision, rel.max())
+
+
+def test_score_2p22_rows_and_determinism(cuda_dev):
+    """n = 2^22 = 4 194 304 anisotropic points: the ordered tensor-core score
+    is bitwise identical across two runs, and rows across the whole range
+    (including those past 64 * 65535 = 4 194 240, where the reference's flash
+    kernel writes the wrong rows) match the FP64 oracle."""
+    from fsk import ops, workloads
+
+    n = 1 << 22
+    x_np = workloads.lowrank_16d(n, seed=0)
+    x = torch.from_numpy(x_np).to(cuda_dev)
+    h = float(ops.silverman(x).item())
+    pdf1, w1 = ops.empscore16(x, h)
+    pdf2, w2 = ops.empscore16(x, h)
+    ops.device_status(cuda_dev)
+    assert torch.equal(pdf1, pdf2) and torch.equal(w1, w2)
+    rows = np.array([0, 1, 77777, 2097152, 4194239, 4194240, 4194241, n - 1])
+    p64, w64 = fp64.empirical_score_rows(x_np, rows, h)
+    pdf = pdf1.cpu().numpy()[rows]
+    w = w1.cpu().numpy()[rows]
+    assert rel_err(pdf, p64).max() < 1e-5, rel_err(pdf, p64).max()
+    np.testing.assert_allclose(w, w64, rtol=1e-5, atol=1e-5 * np.abs(w64).max())
+
+
+def test_kde1d_2p22_by_2p20(cuda_dev):
+    """1-D: 2^22 mixture points, 2^20 grid queries on [-5, 6]; FP64 oracle on
+    64 fixed grid points; atomic and split-K agree."""
+    from fsk import ops, workloads
+
+    x_np = workloads.gmm3_1d(1 << 22, seed=0)
+    q_np = workloads.grid_1d(1 << 20)
+    h = float(R.silverman_bandwidth(x_np))
+    x = torch.from_numpy(x_np).to(cuda_dev)
+    q = torch.from_numpy(q_np).to(cuda_dev)
+    norm = 1.0 / (np.sqrt(2 * np.pi) * h * x_np.size)
+    a = ops.kde1d_sum(q, x, h, out_scale=norm)
+    b = ops.kde1d_sum(q, x, h, out_scale=norm, atomic=True)
+    ops.device_status(cuda_dev)
+    a = a.cpu().numpy().astype(np.float64)
+    b = b.cpu().numpy().astype(np.float64)
+    assert np.isfinite(a).all()
+    assert rel_err(b, a).max() < 1e-5
+    sub = np.linspace(0, q_np.size - 1, 64).astype(np.int64)
+    ref = fp64.density(x_np, q_np[sub], h, q_chunk=64, s_chunk=1 << 16)
+    keep = ref > 1e-30
+    assert rel_err(a[sub][keep], ref[keep]).max() < 1e-5
