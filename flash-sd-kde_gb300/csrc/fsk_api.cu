@@ -327,4 +327,11 @@ int fsk_diag_mma_ts_probe(const float* a, const float* b, float* d, void* stream
   return tc::launch_mma_ts_probe(a, b, d, static_cast<cudaStream_t>(stream));
 }
 
+int fsk_diag_tmem_cp_probe(const float* a, uint32_t* out, void* stream) {
+  if (!a || !out) return FSK_ERR_INVALID_ARGUMENT;
+  int st = check_device();
+  if (st) return st;
+  return tc::launch_tmem_cp_probe(a, out, static_cast<cudaStream_t>(stream));
+}
+
 }  // extern "C"

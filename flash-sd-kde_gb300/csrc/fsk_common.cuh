@@ -366,6 +366,14 @@ __device__ __forceinline__ void tmem_st_wait() {
   asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
+// Asynchronous copy of a 128-row x 256-bit shared-memory tile (described by a
+// matrix descriptor, as for tcgen05.mma) to tensor memory: row r -> lane r,
+// eight consecutive 32-bit columns.  Ordered with the issuing thread's other
+// tcgen05 operations; its completion is tracked by tcgen05.commit.
+__device__ __forceinline__ void tmem_cp_128x256b(uint32_t taddr, uint64_t sdesc) {
+  asm volatile("tcgen05.cp.cta_group::1.128x256b [%0], %1;" ::"r"(taddr), "l"(sdesc) : "memory");
+}
+
 // D[tmem] (+)= A[tmem] * B[smem]^T, kind::f16 (fp16 inputs, FP32 accumulate);
 // A is M x K with row m in TMEM lane m, two fp16 per 32-bit column.
 __device__ __forceinline__ void mma_f16_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b_desc,

@@ -118,6 +118,7 @@ int launch_score16_tc(const float* x, int64_t n, const float* mu, double h, cons
                       double** ppdf_out, double** pw_out, cudaStream_t s);
 int launch_mma_probe(const float* a, const float* b, float* d, cudaStream_t s);
 int launch_mma_ts_probe(const float* a, const float* b, float* d, cudaStream_t s);
+int launch_tmem_cp_probe(const float* a, uint32_t* out, cudaStream_t s);
 int launch_wait_timeout_probe(int* out, cudaStream_t s);
 
 // fp16 core-matrix offset of element (row r, k) in an image whose rows are

@@ -783,6 +783,62 @@ __global__ void __launch_bounds__(128, 1) mma_ts_probe_kernel(const float* __res
 }
 }  // namespace
 
+// ---- layout probe: tcgen05.cp of a query operand image into tensor memory -----
+// A (128 x 32, rounded to fp16) is written in the "hi" operand image layout
+// (64-byte rows, no-swizzle K-major core matrices), copied to TMEM columns
+// 0-15 with two 128x256b copies (K 0-15 at +0 B, K 16-31 at +256 B) and read
+// back with tcgen05.ld: out[r][c] is column c of lane r (two fp16 per word).
+namespace {
+__global__ void __launch_bounds__(128, 1) tmem_cp_probe_kernel(const float* __restrict__ a,
+                                                               uint32_t* __restrict__ out) {
+  __shared__ __align__(1024) uint8_t sa[QT * H_ROW_BYTES];
+  __shared__ uint64_t bar;
+  __shared__ uint32_t slot;
+  const int t = threadIdx.x;
+  const int warp = t >> 5;
+#pragma unroll 4
+  for (int k = 0; k < KH; ++k) put_h(sa, t, k, H_ROW_BYTES, __float2half_rn(a[t * KH + k]));
+  if (t == 0) {
+    mbar_init(&bar, 1);
+    fence_barrier_init();
+  }
+  if (warp == 0) {
+    tmem_alloc(&slot, 32);
+    tmem_relinquish();
+  }
+  fence_proxy_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = slot;
+  if (t == 0) {
+    tmem_cp_128x256b(tbase, smem_desc_kmajor(smem_u32(sa), 128, 8 * H_ROW_BYTES));
+    tmem_cp_128x256b(tbase + 8u, smem_desc_kmajor(smem_u32(sa) + 256, 128, 8 * H_ROW_BYTES));
+    mma_commit(&bar);
+  }
+  __syncwarp();
+  const bool ok = mbar_wait(&bar, 0, 37);
+  tc_fence_after();
+  if (ok) {
+    uint32_t r[16];
+    tmem_ld16(tbase + ((uint32_t)(warp * 32) << 16), r);
+    tmem_ld_wait();
+#pragma unroll
+    for (int j = 0; j < 16; ++j) out[t * 16 + j] = r[j];
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tbase, 32);
+}
+}  // namespace
+
+int launch_tmem_cp_probe(const float* a, uint32_t* out, cudaStream_t s) {
+  tmem_cp_probe_kernel<<<1, 128, 0, s>>>(a, out);
+  count_launch();
+  return cuda_status(cudaGetLastError());
+}
+
 int launch_mma_ts_probe(const float* a, const float* b, float* d, cudaStream_t s) {
   mma_ts_probe_kernel<<<1, 128, 0, s>>>(a, b, d);
   count_launch();

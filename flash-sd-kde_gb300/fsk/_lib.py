@@ -77,6 +77,7 @@ SIGNATURES: dict[str, tuple] = {
     "fsk_launch_count": (_i64, []),
     "fsk_diag_mma_probe": (_int, [_vp, _vp, _vp, _vp]),
     "fsk_diag_mma_ts_probe": (_int, [_vp, _vp, _vp, _vp]),
+    "fsk_diag_tmem_cp_probe": (_int, [_vp, _vp, _vp]),
     "fsk_diag_wait_timeout_probe": (_int, [_vp, _vp]),
     "fsk_diag_pipe_rates": (_int, [_vp, _vp]),
     "fsk_timer_enable": (None, [_int]),

@@ -274,6 +274,20 @@ def mma_ts_probe(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
     return d
 
 
+def tmem_cp_probe(a: torch.Tensor) -> torch.Tensor:
+    """fp16(a) (128,32) in the operand image layout, tcgen05.cp to tensor memory,
+    read back: (128,16) int32 words of packed fp16 pairs."""
+    dev = _device(a.device)
+    a = a.to(device=dev, dtype=torch.float32).contiguous()
+    if a.shape != (128, 32):
+        raise ValueError("probe operand must be (128, 32)")
+    with torch.cuda.device(dev):
+        out = torch.empty((128, 16), dtype=torch.int32, device=dev)
+        st = L.load().fsk_diag_tmem_cp_probe(a.data_ptr(), out.data_ptr(), _stream(dev))
+    L.check(st, "fsk_diag_tmem_cp_probe")
+    return out
+
+
 # ---- learned surrogate (include/fsk.h, "learned surrogate") ----------------------
 MLP_PARAMS = L.FSK_MLP_PARAMS
 

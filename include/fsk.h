@@ -223,6 +223,12 @@ FSK_API int fsk_diag_mma_probe(const float* a, const float* b, float* d, void* s
  * the score kernel's transposed-feature image layout; d is (128,16) FP32
  * row-major, a . b^T of the fp16-rounded inputs. */
 FSK_API int fsk_diag_mma_ts_probe(const float* a, const float* b, float* d, void* stream);
+/* Tensor-memory copy probe, no counterpart in the reference: a (128,32) is
+ * rounded to fp16 into the query operand image layout in shared memory,
+ * copied to tensor memory with two tcgen05.cp 128x256b and read back; out is
+ * (128,16) 32-bit words, word c of row r holding elements 2c (low half) and
+ * 2c+1 (high half) of row r. */
+FSK_API int fsk_diag_tmem_cp_probe(const float* a, uint32_t* out, void* stream);
 /* Failure-path probe, no counterpart in the reference: a kernel waits on an
  * mbarrier nothing arrives on; its bounded wait gives up after about 2 s,
  * writes 0 to *out (device int) and records FSK_ERR_DEVICE_TIMEOUT, which the

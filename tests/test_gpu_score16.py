@@ -39,6 +39,20 @@ def test_mma_ts_probe_layout(cuda_dev):
     assert ((d - ref).abs() <= 2e-6 * scale + 1e-30).all(), float(((d - ref).abs() / scale).max())
 
 
+def test_tmem_cp_probe_layout(cuda_dev):
+    """tcgen05.cp 128x256b of the query operand image (64-byte rows, K-major
+    core matrices) lands row r in TMEM lane r with word c holding the fp16
+    pair (2c, 2c+1): the layout the score kernel's S product reads its A
+    operand in."""
+    from fsk import ops
+
+    g = torch.Generator().manual_seed(5)
+    a = torch.randn(128, 32, generator=g) * 3
+    out = ops.tmem_cp_probe(a.to(cuda_dev)).cpu()
+    want = a.half().contiguous().view(torch.int32)   # (128, 16): pairs of fp16 per word
+    assert torch.equal(out, want)
+
+
 @pytest.mark.parametrize("seed", [2, 3, 4, 10])
 @pytest.mark.parametrize("variant", ["ordered", "symmetric"])
 def test_score_vs_reference(cuda_dev, golden, seed, variant):
