@@ -164,6 +164,7 @@ int fsk_kde16(const float* queries, int64_t m, const float* data, int64_t n, dou
 static size_t empscore_bytes(int64_t n, int variant, int flags) {
   WsCarver c(nullptr, 0);
   take_center(c, n);
+  c.take<double>(reduce_score_scratch_doubles(n));
   size_t b = c.used;
   if (!(flags & FSK_PREC_IEEE)) {
     b = align_up(b, 256) + tc::tc_score16_ws_bytes(tc::plan_score16(n), n);
@@ -196,6 +197,7 @@ int fsk_empscore16(const float* data, int64_t n, double bandwidth, int variant, 
   if (!workspace || workspace_bytes < empscore_bytes(n, variant, flags)) return FSK_ERR_WORKSPACE_TOO_SMALL;
   WsCarver c(workspace, workspace_bytes);
   CenterBufs cb = take_center(c, n);
+  double* rscratch = c.take<double>(reduce_score_scratch_doubles(n));
   launch_mean16(data, n, cb.scratch, cb.mu, cb.mu64, s);
   const bool fm = (flags & FSK_WEIGHTED_FEATURE_MAJOR) != 0;
   const int64_t ws_row = fm ? 1 : FSK_D, ws_col = fm ? n : 1;
@@ -205,21 +207,21 @@ int fsk_empscore16(const float* data, int64_t n, double bandwidth, int variant, 
     st = tc::launch_score16_tc(data, n, cb.mu, bandwidth, pl, c, &ppdf, &pw, s);
     if (st) return st;
     launch_reduce_score(ppdf, pw, (int)(2 * pl.splits), (int)pl.splits, n, cb.mu64, data, pdf_sum,
-                        weighted_sum, ws_row, ws_col, s);
+                        weighted_sum, ws_row, ws_col, rscratch, s);
   } else if (variant == FSK_SCORE_SYMMETRIC) {
     double* apdf = c.take<double>((size_t)n);
     double* aw = c.take<double>((size_t)n * FSK_D);
     launch_zero(apdf, n, s);
     launch_zero(aw, n * FSK_D, s);
     launch_score16_sym_simt(data, n, cb.mu, bandwidth, apdf, aw, s);
-    launch_reduce_score(apdf, aw, 1, 1, n, cb.mu64, nullptr, pdf_sum, weighted_sum, ws_row, ws_col, s);
+    launch_reduce_score(apdf, aw, 1, 1, n, cb.mu64, nullptr, pdf_sum, weighted_sum, ws_row, ws_col, rscratch, s);
   } else {
     const int splits = simt_score16_splits(n);
     double* ppdf = c.take<double>((size_t)splits * n);
     double* pw = c.take<double>((size_t)splits * n * FSK_D);
     launch_score16_simt(data, n, cb.mu, bandwidth, splits, ppdf, pw, s);
     launch_reduce_score(ppdf, pw, splits, splits, n, cb.mu64, nullptr, pdf_sum, weighted_sum, ws_row, ws_col,
-                        s);
+                        rscratch, s);
   }
   return cuda_status(cudaGetLastError());
 }

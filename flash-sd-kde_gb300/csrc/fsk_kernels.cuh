@@ -33,9 +33,11 @@ void launch_reduce_rows(const double* partials, int splits, int64_t m, double sc
 // (pass splits = 1 with atomic accumulators).  w written at w[i*ws_row + k*ws_col].
 // pdf partials [pdf_splits][n], weighted partials [w_splits][n][16] (centred);
 // self_x: the data when the partials leave out the self pair, else nullptr.
+// scratch: reduce_score_scratch_doubles(n) doubles.
+size_t reduce_score_scratch_doubles(int64_t n);
 void launch_reduce_score(const double* ppdf, const double* pw, int pdf_splits, int w_splits, int64_t n,
                          const double* mu64, const float* self_x, float* pdf, float* w, int64_t ws_row,
-                         int64_t ws_col, cudaStream_t s);
+                         int64_t ws_col, double* scratch, cudaStream_t s);
 void launch_debias16(const float* x, int64_t n, const float* pdf, const float* w, int64_t ws_row,
                      int64_t ws_col, double h, double eps, float* debiased, float* score,
                      cudaStream_t s);

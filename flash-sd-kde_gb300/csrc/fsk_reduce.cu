@@ -37,16 +37,27 @@ __global__ void __launch_bounds__(MEAN_THREADS) mean16_partial_kernel(const floa
   }
 }
 
-__global__ void mean16_final_kernel(const double* __restrict__ part, int blocks, int64_t n,
-                                    float* __restrict__ mu, double* __restrict__ mu64) {
-  const int k = threadIdx.x;
-  if (k >= FSK_D) return;
+// One block of MEAN_THREADS: thread t sums the partials b = t/16, t/16 + 16, ...
+// of feature t%16, then each feature's 16 strided sums are added in a fixed
+// order (deterministic).
+__global__ void __launch_bounds__(MEAN_THREADS) mean16_final_kernel(const double* __restrict__ part, int blocks,
+                                                                    int64_t n, float* __restrict__ mu,
+                                                                    double* __restrict__ mu64) {
+  const int k = threadIdx.x % FSK_D;
+  const int l = threadIdx.x / FSK_D;
+  constexpr int L = MEAN_THREADS / FSK_D;
   double s = 0.0;
-  for (int b = 0; b < blocks; ++b) s += part[b * FSK_D + k];
-  const double mean = s / (double)n;
-  const float mf = (float)mean;
-  mu[k] = mf;
-  if (mu64) mu64[k] = (double)mf;  // the shift actually applied (exactly representable)
+  for (int b = l; b < blocks; b += L) s += part[b * FSK_D + k];
+  __shared__ double sh[MEAN_THREADS];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.x < FSK_D) {
+    double t = 0.0;
+    for (int j = 0; j < L; ++j) t += sh[j * FSK_D + threadIdx.x];
+    const float mf = (float)(t / (double)n);
+    mu[threadIdx.x] = mf;
+    if (mu64) mu64[threadIdx.x] = (double)mf;  // the shift actually applied (exactly representable)
+  }
 }
 
 void launch_mean16(const float* x, int64_t n, double* scratch, float* mu, double* mu64,
@@ -55,7 +66,7 @@ void launch_mean16(const float* x, int64_t n, double* scratch, float* mu, double
   blocks = imax(blocks, 1);
   mean16_partial_kernel<<<blocks, MEAN_THREADS, 0, s>>>(x, n, scratch);
   count_launch();
-  mean16_final_kernel<<<1, 32, 0, s>>>(scratch, blocks, n, mu, mu64);
+  mean16_final_kernel<<<1, MEAN_THREADS, 0, s>>>(scratch, blocks, n, mu, mu64);
   count_launch();
 }
 
@@ -78,57 +89,74 @@ void launch_reduce_rows(const double* partials, int splits, int64_t m, double sc
   count_launch();
 }
 
-// pdf = sum of pdf partials, weighted = sum of centred partials + mu * pdf.
-// self_x != nullptr: the partials leave the self pair out; it is added here
-// exactly (phi_ii = 1, weight x_i).
-__global__ void reduce_score_kernel(const double* __restrict__ ppdf, const double* __restrict__ pw,
-                                    int pdf_splits, int w_splits, int64_t n, const double* __restrict__ mu64,
-                                    const float* __restrict__ self_x, float* __restrict__ pdf,
-                                    float* __restrict__ w, int64_t ws_row, int64_t ws_col) {
+// pdf = sum of pdf partials (thread per row; the FP64 sum of the partials,
+// without the self pair, is kept for the weighted pass), then weighted =
+// sum of centred partials + mu * pdf (thread per element, coalesced over the
+// [split][row][16] partials).  self_x != nullptr: the partials leave the self
+// pair out; it is added here exactly (phi_ii = 1, weight x_i).
+__global__ void reduce_score_pdf_kernel(const double* __restrict__ ppdf, int pdf_splits, int64_t n,
+                                        int add_self, float* __restrict__ pdf, double* __restrict__ p_other) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double p = 0.0;
   for (int s = 0; s < pdf_splits; ++s) p += ppdf[(int64_t)s * n + i];
-  const double p_other = p;
-  if (self_x) p += 1.0;
-  pdf[i] = (float)p;
-  for (int k = 0; k < FSK_D; ++k) {
-    double a = 0.0;
-    for (int s = 0; s < w_splits; ++s) a += pw[((int64_t)s * n + i) * FSK_D + k];
-    const double v = self_x ? a + mu64[k] * p_other + (double)self_x[i * FSK_D + k] : a + mu64[k] * p;
-    w[i * ws_row + k * ws_col] = (float)v;
-  }
+  p_other[i] = p;
+  pdf[i] = (float)(add_self ? p + 1.0 : p);
 }
 
-void launch_reduce_score(const double* ppdf, const double* pw, int pdf_splits, int w_splits, int64_t n,
-                         const double* mu64, const float* self_x, float* pdf, float* w, int64_t ws_row,
-                         int64_t ws_col, cudaStream_t s) {
-  const int T = 128;
-  reduce_score_kernel<<<(unsigned)((n + T - 1) / T), T, 0, s>>>(ppdf, pw, pdf_splits, w_splits, n, mu64,
-                                                               self_x, pdf, w, ws_row, ws_col);
-  count_launch();
-}
-
-__global__ void debias16_kernel(const float* __restrict__ x, int64_t n, const float* __restrict__ pdf,
-                                const float* __restrict__ w, int64_t ws_row, int64_t ws_col, double h,
-                                double eps, float* __restrict__ deb, float* __restrict__ score) {
+__global__ void reduce_score_w_kernel(const double* __restrict__ pw, int w_splits, int64_t n,
+                                      const double* __restrict__ mu64, const double* __restrict__ p_other,
+                                      const float* __restrict__ self_x, float* __restrict__ w, int64_t ws_row,
+                                      int64_t ws_col) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n * FSK_D) return;
   const int64_t i = e / FSK_D;
   const int k = (int)(e % FSK_D);
-  const double xi = (double)x[e];
-  const double sc = ((double)w[i * ws_row + k * ws_col] / ((double)pdf[i] + eps) - xi) / (h * h);
-  deb[e] = (float)(xi + 0.5 * h * h * sc);
-  if (score) score[e] = (float)sc;
+  double a = 0.0;
+  for (int s = 0; s < w_splits; ++s) a += pw[(int64_t)s * n * FSK_D + e];
+  const double po = p_other[i];
+  const double v = self_x ? a + mu64[k] * po + (double)self_x[e] : a + mu64[k] * po;
+  w[i * ws_row + k * ws_col] = (float)v;
+}
+
+size_t reduce_score_scratch_doubles(int64_t n) { return (size_t)n; }
+
+void launch_reduce_score(const double* ppdf, const double* pw, int pdf_splits, int w_splits, int64_t n,
+                         const double* mu64, const float* self_x, float* pdf, float* w, int64_t ws_row,
+                         int64_t ws_col, double* scratch, cudaStream_t s) {
+  const int T = 256;
+  reduce_score_pdf_kernel<<<(unsigned)((n + T - 1) / T), T, 0, s>>>(ppdf, pdf_splits, n, self_x != nullptr, pdf,
+                                                                   scratch);
+  count_launch();
+  reduce_score_w_kernel<<<(unsigned)((n * FSK_D + T - 1) / T), T, 0, s>>>(pw, w_splits, n, mu64, scratch, self_x,
+                                                                         w, ws_row, ws_col);
+  count_launch();
+}
+
+// Thread per row, FP64: one reciprocal of (pdf + eps) per row; then per
+// feature score = (w / (pdf + eps) - x) / h^2 and x + h^2/2 * score, which is
+// (x + w / (pdf + eps)) / 2.
+__global__ void debias16_kernel(const float* __restrict__ x, int64_t n, const float* __restrict__ pdf,
+                                const float* __restrict__ w, int64_t ws_row, int64_t ws_col, double inv_h2,
+                                double eps, float* __restrict__ deb, float* __restrict__ score) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double inv = 1.0 / ((double)pdf[i] + eps);
+#pragma unroll
+  for (int k = 0; k < FSK_D; ++k) {
+    const double xi = (double)x[i * FSK_D + k];
+    const double m = (double)w[i * ws_row + k * ws_col] * inv;
+    deb[i * FSK_D + k] = (float)(0.5 * (xi + m));
+    if (score) score[i * FSK_D + k] = (float)((m - xi) * inv_h2);
+  }
 }
 
 void launch_debias16(const float* x, int64_t n, const float* pdf, const float* w, int64_t ws_row,
                      int64_t ws_col, double h, double eps, float* debiased, float* score,
                      cudaStream_t s) {
-  const int T = 256;
-  const int64_t total = n * FSK_D;
-  debias16_kernel<<<(unsigned)((total + T - 1) / T), T, 0, s>>>(x, n, pdf, w, ws_row, ws_col, h, eps,
-                                                               debiased, score);
+  const int T = 128;
+  debias16_kernel<<<(unsigned)((n + T - 1) / T), T, 0, s>>>(x, n, pdf, w, ws_row, ws_col, 1.0 / (h * h), eps,
+                                                           debiased, score);
   count_launch();
 }
 

@@ -78,32 +78,37 @@ __device__ __forceinline__ void put_h(uint8_t* img, int r, int k, int row_bytes,
 // Writes one operand row: H image (features hi + 16 bias columns), M image
 // (features mid) and L image (features lo), v = hi + mid + lo.  own_term:
 // this row's norm term, as three parts in its bias columns; pow_other: the
-// exact power of two multiplying the other side's parts.
+// exact power of two multiplying the other side's parts.  Each 8-element
+// K chunk of a row is 16 contiguous bytes in the core-matrix layout, so the
+// row goes out as 16-byte stores (4 for H, 2 each for M and L).
 __device__ __forceinline__ void write_operand_row(uint8_t* h_img, uint8_t* m_img, uint8_t* l_img, int r,
                                                   const float (&v)[FSK_D], float own_term, float pow_other,
                                                   bool own_first) {
+  __align__(16) __half hrow[KH], mrow[FSK_D], lrow[FSK_D];
 #pragma unroll
-  for (int k = 0; k < FSK_D; ++k) {
-    __half hi, mid, lo;
-    split3_f16(v[k], hi, mid, lo);
-    put_h(h_img, r, k, H_ROW_BYTES, hi);
-    put_h(m_img, r, k, L_ROW_BYTES, mid);
-    put_h(l_img, r, k, L_ROW_BYTES, lo);
-  }
+  for (int k = 0; k < FSK_D; ++k) split3_f16(v[k], hrow[k], mrow[k], lrow[k]);
   __half p0, p1, p2;
   split3_f16(own_term, p0, p1, p2);
   const __half one = __float2half_rn(pow_other);
   const __half zero = __float2half_rn(0.f);
   // bias columns 16..21: A = [2^eb x3 | alpha parts x3], B = [beta parts x3 | 2^ea x3]
   const int own = own_first ? 16 : 19, oth = own_first ? 19 : 16;
-  put_h(h_img, r, own + 0, H_ROW_BYTES, p0);
-  put_h(h_img, r, own + 1, H_ROW_BYTES, p1);
-  put_h(h_img, r, own + 2, H_ROW_BYTES, p2);
-  put_h(h_img, r, oth + 0, H_ROW_BYTES, one);
-  put_h(h_img, r, oth + 1, H_ROW_BYTES, one);
-  put_h(h_img, r, oth + 2, H_ROW_BYTES, one);
+  hrow[own + 0] = p0;
+  hrow[own + 1] = p1;
+  hrow[own + 2] = p2;
+  hrow[oth + 0] = one;
+  hrow[oth + 1] = one;
+  hrow[oth + 2] = one;
 #pragma unroll
-  for (int k = 22; k < KH; ++k) put_h(h_img, r, k, H_ROW_BYTES, zero);
+  for (int k = 22; k < KH; ++k) hrow[k] = zero;
+#pragma unroll
+  for (int c = 0; c < KH / 8; ++c)
+    *reinterpret_cast<uint4*>(h_img + cm_offset(r, 8 * c, H_ROW_BYTES)) = *reinterpret_cast<const uint4*>(hrow + 8 * c);
+#pragma unroll
+  for (int c = 0; c < FSK_D / 8; ++c) {
+    *reinterpret_cast<uint4*>(m_img + cm_offset(r, 8 * c, L_ROW_BYTES)) = *reinterpret_cast<const uint4*>(mrow + 8 * c);
+    *reinterpret_cast<uint4*>(l_img + cm_offset(r, 8 * c, L_ROW_BYTES)) = *reinterpret_cast<const uint4*>(lrow + 8 * c);
+  }
 }
 
 }  // namespace tc
