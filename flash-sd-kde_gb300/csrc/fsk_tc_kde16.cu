@@ -197,12 +197,7 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
         prev_qb = qb;
       }
       const int64_t gi = qb * (NQT * QT) + qt * QT + quarter * 32 + lane;   // padded query index
-      float qx[FSK_D];
-#pragma unroll
-      for (int kk = 0; kk < FSK_D; kk += 4) {
-        const float4 v = *reinterpret_cast<const float4*>(p.qexact + gi * FSK_D + kk);
-        qx[kk] = v.x; qx[kk + 1] = v.y; qx[kk + 2] = v.z; qx[kk + 3] = v.w;
-      }
+      const float* qrow = p.qexact + gi * FSK_D;   // read only by the (rare) exact recompute
       Comp acc{0.f, 0.f};
       float corr = 0.f;
       const int64_t t0 = sp * p.tiles_per_split;
@@ -217,103 +212,112 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
         tc_fence_after();
         const uint8_t* xrows = sB + s * KB_STAGE_BYTES + KB_X_OFFSET + half * (KNT / 2) * (FSK_D * 4);
         float tsum = 0.f;
-#pragma unroll 1
-        for (int c = 0; c < KNT / 64; ++c) {
-          uint32_t r[32];
-          tmem_ld32(tmem_base + lane_off + b * (uint32_t)(NQT * KNT) + (uint32_t)(qt * KNT + half * (KNT / 2) + c * 32),
-                    r);
+        // Both 32-column chunks are loaded before either is processed, so the
+        // accumulator buffer goes back to the MMA issuer as early as possible.
+        uint32_t ra[32], rb[32];
+        {
+          const uint32_t col = tmem_base + lane_off + b * (uint32_t)(NQT * KNT) + (uint32_t)(qt * KNT + half * (KNT / 2));
+          tmem_ld32(col, ra);
+          tmem_ld32(col + 32u, rb);
           tmem_ld_wait();
-          if (c == KNT / 64 - 1) {
-            // accumulator buffer fully read into registers: release it
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&tempty[b * NQT + qt]);
-          }
-          float e[32];
-          if (scaled) {
-#pragma unroll
-            for (int j = 0; j < 32; j += 2) {
-              const float2 v = __fmul2_rn(make_float2(__uint_as_float(r[j]), __uint_as_float(r[j + 1])),
-                                          make_float2(out_mul, out_mul));
-              e[j] = v.x;
-              e[j + 1] = v.y;
-            }
-          } else {
-#pragma unroll
-            for (int j = 0; j < 32; ++j) e[j] = __uint_as_float(r[j]);
-          }
-#pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            float v = ex2_approx(e[j]);
-            // Laplace factor 1 + d/2 - dist/(2h^2) = 9 + a2 ln 2   (a2 = -c2 dist)
-            if (LAPLACE) v *= fmaf(e[j], 0.69314718055994531f, 1.0f + 0.5f * FSK_D);
-            e[j] = v;
-          }
-          const int cvalid = valid - c * 32;   // valid columns of this chunk (may be <= 0 or > 32)
-          if (cvalid < 32) {  // ragged last data tile: drop padding columns
-#pragma unroll
-            for (int j = 0; j < 32; ++j)
-              if (j >= cvalid) e[j] = 0.f;
-          }
-          // packed pairwise sum (f32x2 adds on register pairs)
-          float2 pa = make_float2(e[0], e[1]), pb = make_float2(e[2], e[3]);
-#pragma unroll
-          for (int j = 4; j < 32; j += 4) {
-            pa = __fadd2_rn(pa, make_float2(e[j], e[j + 1]));
-            pb = __fadd2_rn(pb, make_float2(e[j + 2], e[j + 3]));
-          }
-          pa = __fadd2_rn(pa, pb);
-          float cs = pa.x + pa.y;
-          // Near-pair test: a chunk holding more than NEAR_FRACTION of the
-          // running sum (this chunk included) may contain a dominant term.
-          const float run = s_carry + fabsf(acc.s) + fabsf(tsum);
-          const bool trig = fabsf(cs) > (run + fabsf(cs)) * NEAR_FRACTION;
-          if (__any_sync(0xffffffffu, trig)) {
-            // Triggered lanes replace their chunk's largest term by its exact
-            // value.  The argmax rides in the low 5 mantissa bits of each term
-            // (key = |e| with bits[4:0] := column); the chunk is re-summed
-            // from those keyed values, so subtracting the keyed maximum
-            // removes exactly what was added.  All triggered lanes recompute
-            // one pair each, in lock-step.
-            if (trig) {
-              uint32_t key[32];
-              float2 qa = make_float2(0.f, 0.f), qc = make_float2(0.f, 0.f);
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&tempty[b * NQT + qt]);
+        }
+        auto chunk = [&](const uint32_t (&r)[32], const int c) {
+            float e[32];
+            if (scaled) {
 #pragma unroll
               for (int j = 0; j < 32; j += 2) {
-                // terms are >= 0 except with the Laplace factor
-                const float a0 = LAPLACE ? fabsf(e[j]) : e[j], a1 = LAPLACE ? fabsf(e[j + 1]) : e[j + 1];
-                key[j] = (__float_as_uint(a0) & ~31u) | (uint32_t)j;
-                key[j + 1] = (__float_as_uint(a1) & ~31u) | (uint32_t)(j + 1);
-                const float v0 = LAPLACE ? copysignf(__uint_as_float(key[j]), e[j]) : __uint_as_float(key[j]);
-                const float v1 = LAPLACE ? copysignf(__uint_as_float(key[j + 1]), e[j + 1]) : __uint_as_float(key[j + 1]);
-                if (j & 2) qc = __fadd2_rn(qc, make_float2(v0, v1));
-                else qa = __fadd2_rn(qa, make_float2(v0, v1));
+                const float2 v = __fmul2_rn(make_float2(__uint_as_float(r[j]), __uint_as_float(r[j + 1])),
+                                            make_float2(out_mul, out_mul));
+                e[j] = v.x;
+                e[j + 1] = v.y;
               }
-              // max tree over the keys
+            } else {
 #pragma unroll
-              for (int w = 16; w >= 1; w >>= 1)
-#pragma unroll
-                for (int j = 0; j < w; ++j) key[j] = max(key[j], key[j + w]);
-              const uint32_t kmax = key[0];
-              qa = __fadd2_rn(qa, qc);
-              cs = qa.x + qa.y;
-              const int j = (int)(kmax & 31u);
-              float approx = __uint_as_float(kmax);
-              if (LAPLACE) {
-#pragma unroll
-                for (int jj = 0; jj < 32; ++jj)
-                  if (jj == j) approx = copysignf(approx, e[jj]);
-              }
-              const float dist = exact_dist(xrows, c * 32 + j, qx, 0);
-              float ex = exp2_neg_scaled(dist, p.c2, p.c2_lo);
-              if (LAPLACE) ex *= fmaf(-p.c1, dist, 1.0f + 0.5f * FSK_D);
-              if (j >= cvalid) ex = 0.f;
-              corr += ex - approx;
+              for (int j = 0; j < 32; ++j) e[j] = __uint_as_float(r[j]);
             }
-            __syncwarp();
-          }
-          tsum += cs;
-        }
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              float v = ex2_approx(e[j]);
+              // Laplace factor 1 + d/2 - dist/(2h^2) = 9 + a2 ln 2   (a2 = -c2 dist)
+              if (LAPLACE) v *= fmaf(e[j], 0.69314718055994531f, 1.0f + 0.5f * FSK_D);
+              e[j] = v;
+            }
+            const int cvalid = valid - c * 32;   // valid columns of this chunk (may be <= 0 or > 32)
+            if (cvalid < 32) {  // ragged last data tile: drop padding columns
+#pragma unroll
+              for (int j = 0; j < 32; ++j)
+                if (j >= cvalid) e[j] = 0.f;
+            }
+            // packed pairwise sum (f32x2 adds on register pairs)
+            float2 pa = make_float2(e[0], e[1]), pb = make_float2(e[2], e[3]);
+#pragma unroll
+            for (int j = 4; j < 32; j += 4) {
+              pa = __fadd2_rn(pa, make_float2(e[j], e[j + 1]));
+              pb = __fadd2_rn(pb, make_float2(e[j + 2], e[j + 3]));
+            }
+            pa = __fadd2_rn(pa, pb);
+            float cs = pa.x + pa.y;
+            // Near-pair test: a chunk holding more than NEAR_FRACTION of the
+            // running sum (this chunk included) may contain a dominant term.
+            const float run = s_carry + fabsf(acc.s) + fabsf(tsum);
+            const bool trig = fabsf(cs) > (run + fabsf(cs)) * NEAR_FRACTION;
+            if (__any_sync(0xffffffffu, trig)) {
+              // Triggered lanes replace their chunk's largest term by its exact
+              // value.  The argmax rides in the low 5 mantissa bits of each term
+              // (key = |e| with bits[4:0] := column); the chunk is re-summed
+              // from those keyed values, so subtracting the keyed maximum
+              // removes exactly what was added.  All triggered lanes recompute
+              // one pair each, in lock-step.
+              if (trig) {
+                uint32_t key[32];
+                float2 qa = make_float2(0.f, 0.f), qc = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int j = 0; j < 32; j += 2) {
+                  // terms are >= 0 except with the Laplace factor
+                  const float a0 = LAPLACE ? fabsf(e[j]) : e[j], a1 = LAPLACE ? fabsf(e[j + 1]) : e[j + 1];
+                  key[j] = (__float_as_uint(a0) & ~31u) | (uint32_t)j;
+                  key[j + 1] = (__float_as_uint(a1) & ~31u) | (uint32_t)(j + 1);
+                  const float v0 = LAPLACE ? copysignf(__uint_as_float(key[j]), e[j]) : __uint_as_float(key[j]);
+                  const float v1 = LAPLACE ? copysignf(__uint_as_float(key[j + 1]), e[j + 1]) : __uint_as_float(key[j + 1]);
+                  if (j & 2) qc = __fadd2_rn(qc, make_float2(v0, v1));
+                  else qa = __fadd2_rn(qa, make_float2(v0, v1));
+                }
+                // max tree over the keys
+#pragma unroll
+                for (int w = 16; w >= 1; w >>= 1)
+#pragma unroll
+                  for (int j = 0; j < w; ++j) key[j] = max(key[j], key[j + w]);
+                const uint32_t kmax = key[0];
+                qa = __fadd2_rn(qa, qc);
+                cs = qa.x + qa.y;
+                const int j = (int)(kmax & 31u);
+                float approx = __uint_as_float(kmax);
+                if (LAPLACE) {
+#pragma unroll
+                  for (int jj = 0; jj < 32; ++jj)
+                    if (jj == j) approx = copysignf(approx, e[jj]);
+                }
+                float qx[FSK_D];
+#pragma unroll
+                for (int kk = 0; kk < FSK_D; kk += 4) {
+                  const float4 v = *reinterpret_cast<const float4*>(qrow + kk);
+                  qx[kk] = v.x; qx[kk + 1] = v.y; qx[kk + 2] = v.z; qx[kk + 3] = v.w;
+                }
+                const float dist = exact_dist(xrows, c * 32 + j, qx, 0);
+                float ex = exp2_neg_scaled(dist, p.c2, p.c2_lo);
+                if (LAPLACE) ex *= fmaf(-p.c1, dist, 1.0f + 0.5f * FSK_D);
+                if (j >= cvalid) ex = 0.f;
+                corr += ex - approx;
+              }
+              __syncwarp();
+            }
+            tsum += cs;
+        };
+        chunk(ra, 0);
+        chunk(rb, 1);
         acc.add(tsum);
         // the stage's x rows are no longer read by this warp
         __syncwarp();
