@@ -105,24 +105,30 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
   const int64_t sp_begin = u_begin - qb_begin * p.splits;
 
   if (warp == PRODUCER_WARP) {
-    if (lane == 0) {
+    // the whole warp runs the loop (warp-uniform values stay in uniform
+    // registers); lane 0 issues the copies
+    {
       uint32_t& g = n_stage_copies;
       uint32_t& k = n_query_copies;
       int s = 0;
       uint32_t ph = 0;
       int64_t qb = qb_begin, sp = sp_begin;
       for (int64_t u = u_begin; u < u_end; ++u) {
-        if (!mbar_wait(qempty, (k & 1u) ^ 1u, 1)) goto done;
-        mbar_arrive_expect_tx(qready, A_BYTES);
-        bulk_g2s(sA, p.qimg + qb * (int64_t)A_BYTES, A_BYTES, qready);
+        if (!__all_sync(0xffffffffu, mbar_wait(qempty, (k & 1u) ^ 1u, 1))) goto done;
+        if (lane == 0) {
+          mbar_arrive_expect_tx(qready, A_BYTES);
+          bulk_g2s(sA, p.qimg + qb * (int64_t)A_BYTES, A_BYTES, qready);
+        }
         ++k;
         const int64_t t0 = sp * p.tiles_per_split;
         const int64_t t1 = imin<int64_t>(p.n_tiles, t0 + p.tiles_per_split);
         const uint8_t* src = p.ximg + t0 * (int64_t)KB_STAGE_BYTES;
         for (int64_t t = t0; t < t1; ++t, src += KB_STAGE_BYTES) {
-          if (!mbar_wait(&empty[s], ph ^ 1u, 2)) goto done;
-          mbar_arrive_expect_tx(&full[s], KB_STAGE_BYTES);
-          bulk_g2s(sB + s * KB_STAGE_BYTES, src, KB_STAGE_BYTES, &full[s]);
+          if (!__all_sync(0xffffffffu, mbar_wait(&empty[s], ph ^ 1u, 2))) goto done;
+          if (lane == 0) {
+            mbar_arrive_expect_tx(&full[s], KB_STAGE_BYTES);
+            bulk_g2s(sB + s * KB_STAGE_BYTES, src, KB_STAGE_BYTES, &full[s]);
+          }
           ++g;
           if (++s == NS) {
             s = 0;
@@ -140,8 +146,8 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
     // barriers: a tile's MMAs wait only for the 8 epilogue warps reading that
     // tile.  The per-tile path is kept to the waits, the MMAs and the commits
     // (descriptors of stage s = stage 0 + s * 1 KiB in the 16-byte address
-    // field).
-    if (lane == 0) {
+    // field).  The whole warp runs the loop; lane 0 issues and commits.
+    {
       const uint32_t idesc = idesc_f16_f32(QT, KNT);
       const int a = (warp == MMA_WARP) ? 0 : 1;
       const uint32_t as = smem_u32(sA + a * A_TILE_BYTES);
@@ -157,24 +163,28 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
       int s = 0;
       int64_t sp = sp_begin;
       for (int64_t u = u_begin; u < u_end; ++u, ++k) {
-        if (!mbar_wait(qready, k & 1u, 3)) goto done;
+        if (!__all_sync(0xffffffffu, mbar_wait(qready, k & 1u, 3))) goto done;
         const int64_t t0 = sp * p.tiles_per_split;
         const int nt = (int)(imin<int64_t>(p.n_tiles, t0 + p.tiles_per_split) - t0);
         for (int i = 0; i < nt; ++i, ++g) {
           const uint32_t b = g & 1u;
-          if (!mbar_wait(&full[s], ph, 4)) goto done;
-          if (!mbar_wait(&tempty[b * NQT + a], ((g >> 1) & 1u) ^ 1u, 5)) goto done;
+          if (!__all_sync(0xffffffffu, mbar_wait(&full[s], ph, 4))) goto done;
+          if (!__all_sync(0xffffffffu, mbar_wait(&tempty[b * NQT + a], ((g >> 1) & 1u) ^ 1u, 5))) goto done;
           tc_fence_after();
           const uint64_t so = (uint64_t)(s * (KB_STAGE_BYTES >> 4));
-          mma_s_tile<true>(d0 + b * (uint32_t)(NQT * KNT), a_h, a_m, a_l, b_h0 + so, b_m0 + so, b_l0 + so, idesc);
-          mma_commit(&tfull[b * NQT + a]);
-          mma_commit(&empty[s]);
+          if (lane == 0) {
+            mma_s_tile<true>(d0 + b * (uint32_t)(NQT * KNT), a_h, a_m, a_l, b_h0 + so, b_m0 + so, b_l0 + so, idesc);
+            mma_commit(&tfull[b * NQT + a]);
+            mma_commit(&empty[s]);
+          }
+          __syncwarp();
           if (++s == NS) {
             s = 0;
             ph ^= 1u;
           }
         }
-        mma_commit(qempty);
+        if (lane == 0) mma_commit(qempty);
+        __syncwarp();
         if (++sp == p.splits) sp = 0;
       }
     }

@@ -217,24 +217,35 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
   const int64_t u_end = (int64_t)(blockIdx.x + 1) * units / gridDim.x;
 
   if (warp == S_PRODUCER_WARP) {
-    if (lane == 0) {
+    // whole warp runs the loop (32-bit stage / phase counters), lane 0 copies
+    {
       int64_t& g = n_stage_copies;
       int64_t& k = n_query_copies;
+      int st = 0;
+      uint32_t ph = 0;
       for (int64_t u = u_begin; u < u_end; ++u) {
         const int64_t qb = u / p.splits, sp = u % p.splits;
-        if (!mbar_wait(qempty, (uint32_t)((k & 1) ^ 1), 21)) goto done;
-        mbar_arrive_expect_tx(qready, S_A_BYTES + S_QX_BYTES);
-        bulk_g2s(sA, p.qimg + qb * (int64_t)S_A_BYTES, S_A_BYTES, qready);
-        bulk_g2s(smem_raw + S_QX_OFFSET, p.qexact + qb * (int64_t)(SNQT * QT * FSK_D), S_QX_BYTES, qready);
+        if (!__all_sync(0xffffffffu, mbar_wait(qempty, (uint32_t)((k & 1) ^ 1), 21))) goto done;
+        if (lane == 0) {
+          mbar_arrive_expect_tx(qready, S_A_BYTES + S_QX_BYTES);
+          bulk_g2s(sA, p.qimg + qb * (int64_t)S_A_BYTES, S_A_BYTES, qready);
+          bulk_g2s(smem_raw + S_QX_OFFSET, p.qexact + qb * (int64_t)(SNQT * QT * FSK_D), S_QX_BYTES, qready);
+        }
         ++k;
         const int64_t t0 = sp * p.tiles_per_split;
         const int64_t t1 = imin<int64_t>(p.n_tiles, t0 + p.tiles_per_split);
-        for (int64_t t = t0; t < t1; ++t) {
-          const int s = (int)(g % SNS);
-          if (!mbar_wait(&empty[s], (uint32_t)(((g / SNS) & 1) ^ 1), 22)) goto done;
-          mbar_arrive_expect_tx(&full[s], S_STAGE_BYTES);
-          bulk_g2s(sB + s * S_STAGE_BYTES, p.ximg + t * (int64_t)S_STAGE_BYTES, S_STAGE_BYTES, &full[s]);
+        const uint8_t* src = p.ximg + t0 * (int64_t)S_STAGE_BYTES;
+        for (int64_t t = t0; t < t1; ++t, src += S_STAGE_BYTES) {
+          if (!__all_sync(0xffffffffu, mbar_wait(&empty[st], ph ^ 1u, 22))) goto done;
+          if (lane == 0) {
+            mbar_arrive_expect_tx(&full[st], S_STAGE_BYTES);
+            bulk_g2s(sB + st * S_STAGE_BYTES, src, S_STAGE_BYTES, &full[st]);
+          }
           ++g;
+          if (++st == SNS) {
+            st = 0;
+            ph ^= 1u;
+          }
         }
       }
     }
@@ -242,8 +253,10 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
     // S(g) of one query tile for every tile, up to NBUF tiles ahead of W:
     // buffer g % NBUF is reused once both W parts of tile g - NBUF have read
     // its weights (sfree).  S and W are issued by different threads because
-    // tcgen05.commit tracks every earlier MMA of its thread.
-    if (lane == 0) {
+    // tcgen05.commit tracks every earlier MMA of its thread.  The whole warp
+    // runs the loop (warp-uniform values stay in uniform registers); lane 0
+    // issues the MMAs and commits.
+    {
       const int a = warp == S_MMA_WARP ? 0 : 1;
       const uint32_t idesc_s = idesc_f16_f32(QT, NT);
       const uint32_t a_h = tmem_base + (uint32_t)(T_A + a * 32);   // hi: features | bias; mid at +16, lo at +24
@@ -260,33 +273,39 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
         const int s = gs % SNS;
         const int b = gs % NBUF;
         if (cs.t == cs.t0) {   // first tile of a unit: its A operand in TMEM
-          if (!mbar_wait(&aready[a], (uint32_t)(ku & 1), 23)) goto done;
+          if (!__all_sync(0xffffffffu, mbar_wait(&aready[a], (uint32_t)(ku & 1), 23))) goto done;
           ++ku;
         }
-        if (gs >= NBUF && !mbar_wait(&sfree[b * SNQT + a], (uint32_t)(((gs / NBUF) - 1) & 1), 25)) goto done;
-        if (!mbar_wait(&full[s], (uint32_t)((gs / SNS) & 1), 24)) goto done;
+        if (gs >= NBUF &&
+            !__all_sync(0xffffffffu, mbar_wait(&sfree[b * SNQT + a], (uint32_t)(((gs / NBUF) - 1) & 1), 25)))
+          goto done;
+        if (!__all_sync(0xffffffffu, mbar_wait(&full[s], (uint32_t)((gs / SNS) & 1), 24))) goto done;
         tc_fence_after();
         const uint64_t so = (uint64_t)((s * S_STAGE_BYTES) >> 4);
         const uint32_t d = tmem_base + (uint32_t)(T_S + b * (SNQT * NT) + a * NT);
         const uint64_t b_h = dh0 + so;
         // three-part product, small terms first (the order of mma_s_tile<true>)
         const uint64_t b_m = dm0 + so, b_l = dl0 + so;
-        mma_f16_ts(d, a_h + 16u, b_m, idesc_s, 0u);                    // mid . mid
-        mma_f16_ts(d, a_h, b_l, idesc_s, 1u);                          // hi . lo
-        mma_f16_ts(d, a_h + 24u, b_h, idesc_s, 1u);                    // lo . hi
-        mma_f16_ts(d, a_h, b_m, idesc_s, 1u);                          // hi . mid
-        mma_f16_ts(d, a_h + 16u, b_h, idesc_s, 1u);                    // mid . hi
-        mma_f16_ts(d, a_h, b_h, idesc_s, 1u);                          // hi . hi
-        mma_f16_ts(d, a_h + 8u, b_h + (uint64_t)(256 >> 4), idesc_s, 1u);   // bias . bias
-        mma_commit(&tfull[b * SNQT + a]);
+        if (lane == 0) {
+          mma_f16_ts(d, a_h + 16u, b_m, idesc_s, 0u);                    // mid . mid
+          mma_f16_ts(d, a_h, b_l, idesc_s, 1u);                          // hi . lo
+          mma_f16_ts(d, a_h + 24u, b_h, idesc_s, 1u);                    // lo . hi
+          mma_f16_ts(d, a_h, b_m, idesc_s, 1u);                          // hi . mid
+          mma_f16_ts(d, a_h + 16u, b_h, idesc_s, 1u);                    // mid . hi
+          mma_f16_ts(d, a_h, b_h, idesc_s, 1u);                          // hi . hi
+          mma_f16_ts(d, a_h + 8u, b_h + (uint64_t)(256 >> 4), idesc_s, 1u);   // bias . bias
+          mma_commit(&tfull[b * SNQT + a]);
+        }
+        __syncwarp();
         ++gs;
         cs.next();
       }
     }
   } else if (warp >= W_MMA_WARP) {
     // W(g) of one (query tile, weight part) once the epilogue warps of that
-    // query tile have stored tile g's weights.
-    if (lane == 0) {
+    // query tile have stored tile g's weights (whole warp runs the loop, lane
+    // 0 issues).
+    {
       const int wi = warp - W_MMA_WARP;
       const int a = wi >> 1, part = wi & 1;   // part 0: hi weights x [X_hi | X_lo]; 1: lo weights x X_hi
       const uint32_t idesc_w = idesc_f16_f32(QT, part ? WN_LO : WN);
@@ -301,24 +320,27 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
         const bool first = pos == 0;
         const bool last = pos == S_GROUP - 1 || cw.t == cw.t1 - 1;
         const int par = grp & 1;
-        if (first && !mbar_wait(&wempty[par * SNQT + a], (uint32_t)(((grp >> 1) & 1) ^ 1), 26)) goto done;
-        if (!mbar_wait(&pready[b * SNQT + a], (uint32_t)((gw / NBUF) & 1), 27)) goto done;
+        if (first &&
+            !__all_sync(0xffffffffu, mbar_wait(&wempty[par * SNQT + a], (uint32_t)(((grp >> 1) & 1) ^ 1), 26)))
+          goto done;
+        if (!__all_sync(0xffffffffu, mbar_wait(&pready[b * SNQT + a], (uint32_t)((gw / NBUF) & 1), 27))) goto done;
         tc_fence_after();
         const uint64_t xd0 = dx0 + (uint64_t)((s * S_STAGE_BYTES) >> 4);
         const uint32_t ph = tmem_base + (uint32_t)(T_S + b * (SNQT * NT) + a * NT + part * 16);
         const uint32_t d = tmem_base + (uint32_t)(T_W + par * (SNQT * W_TILE_COLS) + a * W_TILE_COLS + part * WN);
+        if (lane == 0) {
 #pragma unroll
-        for (int ks = 0; ks < NT / 16; ++ks) {
-          // data columns 16 ks .. +15: column half ks/2; weights hi at +0, lo at +16
-          const uint32_t wa = ph + (uint32_t)(32 * (ks >> 1) + 8 * (ks & 1));
-          mma_f16_ts(d, wa, xd0 + (uint64_t)(ks * (256 >> 4)), idesc_w, (first && ks == 0) ? 0u : 1u);
+          for (int ks = 0; ks < NT / 16; ++ks) {
+            // data columns 16 ks .. +15: column half ks/2; weights hi at +0, lo at +16
+            const uint32_t wa = ph + (uint32_t)(32 * (ks >> 1) + 8 * (ks & 1));
+            mma_f16_ts(d, wa, xd0 + (uint64_t)(ks * (256 >> 4)), idesc_w, (first && ks == 0) ? 0u : 1u);
+          }
+          mma_commit(&sfree[b * SNQT + a]);
+          mma_commit(&empty[s]);
+          if (last) mma_commit(&wfull[par * SNQT + a]);
         }
-        mma_commit(&sfree[b * SNQT + a]);
-        mma_commit(&empty[s]);
-        if (last) {
-          mma_commit(&wfull[par * SNQT + a]);
-          ++grp;
-        }
+        __syncwarp();
+        if (last) ++grp;
         ++gw;
         cw.next();
       }
