@@ -213,10 +213,13 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
       const int64_t t0 = sp * p.tiles_per_split;
       const int nt = (int)(imin<int64_t>(p.n_tiles, t0 + p.tiles_per_split) - t0);
       // columns of this thread's half of tile t0 + i: first data index and valid count
-      int64_t col0 = t0 * KNT + half * (KNT / 2);
-      for (int i = 0; i < nt; ++i, ++g, col0 += KNT) {
+      // valid columns of this thread's half of the last (possibly ragged) data
+      // tile; every other tile has KNT / 2
+      const int last_i = (int)(p.n_tiles - 1 - t0);
+      const int last_valid = (int)imin<int64_t>(KNT / 2, p.n - ((p.n_tiles - 1) * KNT + half * (KNT / 2)));
+      for (int i = 0; i < nt; ++i, ++g) {
         const uint32_t b = g & 1u;
-        const int valid = (int)imin<int64_t>(KNT / 2, p.n - col0);   // may be <= 0
+        const int valid = i == last_i ? last_valid : KNT / 2;   // may be <= 0 on the last tile
         // (a timed-out wait ends the whole warp: it must stay converged)
         if (!__all_sync(0xffffffffu, mbar_wait(&tfull[b * NQT + qt], (g >> 1) & 1u, 6))) goto done;
         tc_fence_after();

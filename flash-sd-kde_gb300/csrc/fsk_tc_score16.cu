@@ -368,6 +368,10 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
         *reinterpret_cast<float4*>(wcorr + par * WC_PAR + half * WC_HALF + wc_row + k) =
             make_float4(0.f, 0.f, 0.f, 0.f);
     int g = 0, grp = 0, k_unit = 0;
+    int s = 0;   // data stage of tile g (g % SNS, advanced per tile)
+    // valid columns of the last (possibly ragged) data tile; every other tile has NT
+    const int last_t = (int)p.n_tiles - 1;
+    const int last_valid = (int)(p.n - (int64_t)last_t * NT);
     int prev_qb = -1;
     float s_carry = 0.f;
     const int splits = (int)p.splits, tps = (int)p.tiles_per_split, n_tiles = (int)p.n_tiles;
@@ -418,10 +422,9 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
       const int t0 = sp * tps;
       const int t1 = imin(n_tiles, t0 + tps);
       bool pend = false;     // a W group ended at the previous tile and is not read yet
-      for (int t = t0; t < t1; ++t, ++g) {
-        const int s = g % SNS;
+      for (int t = t0; t < t1; ++t, ++g, s = (s + 1 == SNS) ? 0 : s + 1) {
         const int b = g % NBUF;
-        const int valid = (int)imin<int64_t>(NT, p.n - (int64_t)t * NT);
+        const int valid = t == last_t ? last_valid : NT;
         if (!__all_sync(0xffffffffu, mbar_wait(&tfull[b * SNQT + qt], (uint32_t)((g / NBUF) & 1), 28))) goto done;
         tc_fence_after();
         const uint8_t* stage = sB + s * S_STAGE_BYTES;
