@@ -87,6 +87,20 @@ def test_ragged_and_tiny_shapes(cuda_dev, m, n, precision):
     assert rel_err(out, truth).max() < 1e-5
 
 
+@pytest.mark.parametrize("m,n", [(256, 64), (257, 65), (511, 191), (512, 192), (513, 193), (255, 320),
+                                 (256, 383), (1, 384), (300, 385), (768, 1000)])
+def test_tile_boundary_shapes(cuda_dev, m, n):
+    """Query counts around the 256-query work unit and data counts around the
+    128-point tile and its 64-point column halves (tensor-core path)."""
+    rng = np.random.default_rng(m * 131 + n)
+    x = rng.standard_normal((n, 16)).astype(np.float32)
+    q = (x[rng.integers(0, n, m)] + 0.3 * rng.standard_normal((m, 16))).astype(np.float32)
+    h = 0.7
+    out = _kde(cuda_dev, q, x, h)
+    truth = fp64.density(x, q, h)
+    assert rel_err(out, truth).max() < 1e-5
+
+
 @pytest.mark.parametrize("precision", PRECISIONS)
 def test_offset_heavy_tail_cancellation(cuda_dev, precision):
     """Student-t data with a +100 offset: the norm expansion cancels

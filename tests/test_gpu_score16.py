@@ -124,6 +124,22 @@ def test_fit_transform_backends(cuda_dev, golden):
     _close(g["score"], s64, rtol=1e-3, floor=1e-3)
 
 
+@pytest.mark.parametrize("n", [1, 2, 63, 64, 65, 255, 256, 257, 300, 513])
+def test_score_tile_boundary_shapes(cuda_dev, n):
+    """Point counts around the 64-point data tile, its 32-column halves and
+    the 256-row work unit: pdf and weighted sums vs the FP64 oracle."""
+    from fsk import ops
+
+    rng = np.random.default_rng(n + 17)
+    xs = (rng.standard_normal((n, 16)) * 1.5).astype(np.float32)
+    h = 0.8
+    pdf, w = ops.empscore16(torch.from_numpy(xs).to(cuda_dev), h)
+    ops.device_status(cuda_dev)
+    p64, w64, _ = fp64.empirical_score(xs, h)
+    _close(pdf.cpu().numpy(), p64, rtol=2e-6, floor=0)
+    _close(w.cpu().numpy(), w64, rtol=2e-6, floor=2e-6)
+
+
 def test_score_offset_data(cuda_dev):
     """Offset heavy-tailed data: weighted sums and debiased points vs FP64."""
     from fsk import ops, workloads
