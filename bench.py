@@ -72,7 +72,7 @@ def parse():
     ap.add_argument("--sur-train", type=int, default=262144, help="surrogate workload: exact SD-KDE fit points")
     ap.add_argument("--sur-pairs", type=int, default=4_000_000, help="surrogate workload: training pairs")
     ap.add_argument("--sur-eval", type=int, default=1_000_000, help="surrogate workload: held-out queries")
-    ap.add_argument("--op", choices=["kde16", "score16"], default=None,
+    ap.add_argument("--op", choices=["kde16", "kde16_logexact", "score16"], default=None,
                     help="time one operation alone on n GMM8 points (profiling case; no contract line)")
     ap.add_argument("--n", type=int, default=N_TRAIN, help="points for --op (queries = data)")
     return ap.parse_args()
@@ -465,7 +465,11 @@ def surrogate_workload(args, dev) -> dict:
     ms_gated, (logp, served) = timed(lambda: sur.score_samples(q, return_served=True))
     ms_sur, _ = timed(lambda: sur.predict(q))
     ops.device_status(dev)
-    fin = torch.isfinite(exact)          # far queries can underflow the FP32 kernel sum (log 0)
+    # the exact path recomputes queries whose FP32 sum underflows (log 0 in a plain FP32 sum)
+    norm = 1.0 / ((2.0 * math.pi) ** 8 * h ** 16 * deb.shape[0])
+    plain = ops.kde16_sum(q, deb, h, out_scale=norm, log_eps=0.0)
+    recomputed = int((~torch.isfinite(plain)).sum())
+    fin = torch.isfinite(exact)
     rel = (torch.exp((logp - exact).double()) - 1).abs()
     srv = served.bool() & fin
     n = q.shape[0]
@@ -486,7 +490,8 @@ def surrogate_workload(args, dev) -> dict:
         "median_rel_density_err_all_surrogate": float(
             (torch.exp((sur.predict(q)[0] - exact).double()) - 1).abs()[fin].median()),
         "median_abs_log_err_in_support_surrogate": float((sur.predict(q)[0] - exact)[:half].abs().median()),
-        "exact_underflow_queries": int((~fin).sum()),
+        "exact_recomputed_underflow_queries": recomputed,
+        "exact_nonfinite_queries": int((~fin).sum()),
         "spread_tol": sur.spread_tol, "r2_max": sur.r2_max_,
     }
 
@@ -504,7 +509,9 @@ def run_surrogate(args) -> None:
 def run_op(args) -> None:
     """One operation alone (the profiling case for ncu captures): n GMM8
     points as data and as queries, Silverman bandwidth, W warm-up and K timed
-    launches with CUDA events on the launching stream."""
+    launches with CUDA events on the launching stream.  kde16_logexact: exact
+    log-densities with half the queries moved 60 bandwidths away from the data
+    (every term of those underflows FP32, so they take the shifted recompute)."""
     import torch
 
     import __graft_entry__ as ge
@@ -517,6 +524,10 @@ def run_op(args) -> None:
     h = float(ops.silverman(x).item())
     if args.op == "kde16":
         fn = lambda: ops.kde16_sum(x, x, h)
+    elif args.op == "kde16_logexact":
+        q = x.clone()
+        q[::2] += 60.0 * h / 4.0      # offset 15 h per feature: 60 h away in 16-D
+        fn = lambda: ops.kde16_sum(q, x, h, log_exact=True)
     else:
         fn = lambda: ops.empscore16(x, h)
     for _ in range(args.warmup):

@@ -40,7 +40,7 @@ bool bad_bw(double h) { return !(h > 0.0) || !isfinite(h); }
 
 // ---- 16-D KDE workspace plan ---------------------------------------------------
 struct Kde16Plan {
-  bool ieee, atomic;
+  bool ieee, atomic, log_exact;
   int simt_splits;
   tc::TcPlan tcp;
 };
@@ -49,6 +49,7 @@ Kde16Plan plan16(int64_t m, int64_t n, int flags) {
   Kde16Plan p{};
   p.ieee = (flags & FSK_PREC_IEEE) != 0;
   p.atomic = (flags & FSK_ATOMIC) != 0;
+  p.log_exact = (flags & FSK_OUT_LOG_EXACT) != 0;
   if (p.ieee) p.simt_splits = simt_kde16_splits(m, n);
   else p.tcp = tc::plan_kde16(m, n);
   return p;
@@ -76,10 +77,18 @@ size_t kde16_bytes(int64_t m, int64_t n, const Kde16Plan& p) {
   } else {
     c.used = align_up(c.used, 256) + tc::tc_kde16_ws_bytes(p.tcp, m, p.atomic);
   }
+  if (p.log_exact) take_logexact(c, m, nullptr);
   return align_up(c.used, 256);
 }
 
-constexpr int KNOWN_FLAGS = FSK_PREC_IEEE | FSK_LAPLACE | FSK_OUT_LOG | FSK_ATOMIC | FSK_WEIGHTED_FEATURE_MAJOR;
+constexpr int KNOWN_FLAGS =
+    FSK_PREC_IEEE | FSK_LAPLACE | FSK_OUT_LOG | FSK_ATOMIC | FSK_WEIGHTED_FEATURE_MAJOR | FSK_OUT_LOG_EXACT;
+
+// FSK_OUT_LOG_EXACT: only with FSK_OUT_LOG, out_eps = 0 and m < 2^32 (list indices)
+bool bad_log_exact(int flags, double out_eps, int64_t m) {
+  if (!(flags & FSK_OUT_LOG_EXACT)) return false;
+  return !(flags & FSK_OUT_LOG) || out_eps != 0.0 || m >= (int64_t(1) << 32);
+}
 
 }  // namespace
 }  // namespace fsk
@@ -129,6 +138,7 @@ int fsk_kde16(const float* queries, int64_t m, const float* data, int64_t n, dou
               void* stream) {
   if (!queries || !data || !out || m < 1 || n < 1 || bad_bw(bandwidth)) return FSK_ERR_INVALID_ARGUMENT;
   if (flags & ~KNOWN_FLAGS) return FSK_ERR_INVALID_ARGUMENT;
+  if (bad_log_exact(flags, out_eps, m)) return FSK_ERR_INVALID_ARGUMENT;
   int st = check_device();
   if (st) return st;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -152,7 +162,14 @@ int fsk_kde16(const float* queries, int64_t m, const float* data, int64_t n, dou
     if (st) return st;
     splits = p.atomic ? 1 : (int)p.tcp.part_rows;
   }
-  launch_reduce_rows(part, splits, m, out_scale, out_eps, (flags & FSK_OUT_LOG) != 0, out, s);
+  if (p.log_exact) {
+    LogExactBufs lb;
+    take_logexact(c, m, &lb);
+    if (!c.fits()) return FSK_ERR_WORKSPACE_TOO_SMALL;
+    launch_reduce_logexact(queries, m, data, n, bandwidth, laplace, part, splits, out_scale, lb, out, s);
+  } else {
+    launch_reduce_rows(part, splits, m, out_scale, out_eps, (flags & FSK_OUT_LOG) != 0, out, s);
+  }
   return cuda_status(cudaGetLastError());
 }
 

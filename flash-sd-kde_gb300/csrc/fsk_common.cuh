@@ -41,6 +41,7 @@ enum KernelId {
   K_KDE1D_SCORE = 6,
   K_SCORE16_TC = 7,
   K_MLP_INFER = 9,   // work unit: one (query, ensemble member) evaluation
+  K_KDE16_LOGSPACE = 10,   // shifted recompute of underflowing queries (work not known on the host)
 };
 
 // RAII bracket of one kernel launch with CUDA events on its stream when the

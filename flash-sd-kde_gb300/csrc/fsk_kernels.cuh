@@ -47,6 +47,21 @@ void launch_reduce_kde1d_score(const double* p0, const double* p1, int splits, i
                                cudaStream_t s);
 void launch_zero(double* p, int64_t count, cudaStream_t s);
 
+// ---- fsk_logspace.cu ------------------------------------------------------------
+// FSK_OUT_LOG_EXACT: log(scale * sum) per query from the split partials; the
+// queries whose sum underflows are recomputed with a running-minimum shift.
+#define FSK_LS_PARTS 8   // data parts per recomputed query (partial rows)
+struct LogExactBufs {
+  uint32_t* count;   // listed queries
+  uint32_t* list;    // [m] query indices
+  float* pd;         // [FSK_LS_PARTS][m] smallest squared distance per part
+  double* ps;        // [FSK_LS_PARTS][m] shifted sums per part
+};
+void take_logexact(WsCarver& c, int64_t m, LogExactBufs* b);
+void launch_reduce_logexact(const float* q, int64_t m, const float* x, int64_t n, double h, bool laplace,
+                            const double* partials, int splits, double scale, const LogExactBufs& b, float* out,
+                            cudaStream_t s);
+
 // ---- fsk_silverman.cu -----------------------------------------------------------
 size_t silverman_ws_bytes(int64_t n, int d);
 int run_silverman(const float* x, int64_t n, int d, int rule, double* h_out, void* ws, size_t ws_bytes,

@@ -3,7 +3,9 @@
 fit(X) resolves the bandwidth (Silverman's rule evaluated on the GPU in FP64),
 stores the data or the SD-KDE-debiased data on the device; score_samples(X)
 returns log(density + eps) as a numpy array, with the log taken in FP64 in
-the kernels' split reduction.
+the kernels' split reduction (with log_space=True, an addition of this
+package, the exact log-density without the eps floor, also where the density
+underflows FP32).
 """
 from __future__ import annotations
 
@@ -40,6 +42,10 @@ class FlashSDKDE:
     use_precomputed_norms: bool = True
     autotune: bool = True
     eps: float = DEFAULT_EPS
+    # Not in the reference: score_samples returns the exact log-density
+    # (no log(density + eps) floor, no underflow for out-of-support queries;
+    # 16-D only).  Default off, so results match the reference.
+    log_space: bool = False
 
     bandwidth_: float | None = field(default=None, init=False)
     n_features_in_: int | None = field(default=None, init=False)
@@ -83,7 +89,8 @@ class FlashSDKDE:
             q = q[:, 0].contiguous()
         log_density = _kde_eval_impl(self._fit_eval_data, q, self.bandwidth_, device=dev,
                                      precision_mode=self.precision_mode, kde_backend=self.kde_backend,
-                                     apply_laplacian_correction=False, log_eps=float(self.eps))
+                                     apply_laplacian_correction=False, log_eps=float(self.eps),
+                                     log_exact=bool(self.log_space))
         return log_density.detach().cpu().numpy()
 
     def score(self, X: np.ndarray, y=None) -> float:

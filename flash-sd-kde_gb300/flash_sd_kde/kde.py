@@ -61,7 +61,7 @@ def _require_cuda(device, name: str) -> torch.device:
 
 
 def _kde_eval_impl(data, queries, bandwidth, *, device, precision_mode, kde_backend,
-                   apply_laplacian_correction, log_eps=None):
+                   apply_laplacian_correction, log_eps=None, log_exact=False):
     validate_precision_mode(precision_mode)
     validate_kde_backend(kde_backend)
     if bandwidth <= 0:
@@ -70,6 +70,8 @@ def _kde_eval_impl(data, queries, bandwidth, *, device, precision_mode, kde_back
     atomic = kde_backend == KDE_BACKEND_ATOMIC
     ndim = _infer_ndim(data)
     if ndim == 1:
+        if log_exact:
+            raise ValueError("exact log-densities are available for 16-D data only.")
         train = ops.as_vector(data, device)
         query = ops.as_vector(queries, device)
         n_data = train.numel()
@@ -87,7 +89,8 @@ def _kde_eval_impl(data, queries, bandwidth, *, device, precision_mode, kde_back
         norm = 1.0 / ((2.0 * math.pi) ** (ND_FEATURES / 2.0) * (bandwidth ** ND_FEATURES) * n_data)
         prec = "ieee" if precision_mode == PRECISION_FP32_IEEE else "tensor"
         return ops.kde16_sum(query, train, bandwidth, precision=prec, laplace=apply_laplacian_correction,
-                             atomic=atomic, out_scale=norm, log_eps=log_eps)
+                             atomic=atomic, out_scale=norm, log_eps=None if log_exact else log_eps,
+                             log_exact=log_exact)
     raise ValueError("data must be 1D or 2D.")
 
 
@@ -111,9 +114,17 @@ def kde_eval(
 def kde_eval_log(data, queries, bandwidth: float, *, eps: float = DEFAULT_EPS, device="cuda",
                  precision_mode: str = DEFAULT_PRECISION_MODE, kde_backend: str = DEFAULT_KDE_BACKEND) -> torch.Tensor:
     """log(kde_eval(...) + eps) with the log taken in FP64 inside the reduction
-    (what FlashSDKDE.score_samples returns, flash_sd_kde/estimator.py:104-115)."""
+    (what FlashSDKDE.score_samples returns, flash_sd_kde/estimator.py:104-115).
+
+    eps = 0 (16-D): the exact log-density, also where the density underflows
+    FP32 (out-of-support queries are recomputed with a running-minimum shift
+    and the log is assembled in FP64), instead of log(0) = -inf.
+    """
+    if eps < 0:
+        raise ValueError("eps must be non-negative.")
     return _kde_eval_impl(data, queries, bandwidth, device=device, precision_mode=precision_mode,
-                          kde_backend=kde_backend, apply_laplacian_correction=False, log_eps=float(eps))
+                          kde_backend=kde_backend, apply_laplacian_correction=False, log_eps=float(eps),
+                          log_exact=eps == 0)
 
 
 def kde_eval_linearized(

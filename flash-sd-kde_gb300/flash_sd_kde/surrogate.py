@@ -68,7 +68,9 @@ class SurrogateKDE:
         norm = 1.0 / ((2.0 * math.pi) ** (ND_FEATURES / 2.0) * h ** ND_FEATURES * n)
         out = torch.empty(queries.shape[0], dtype=torch.float32, device=queries.device)
         for s in range(0, queries.shape[0], chunk):
-            ops.kde16_sum(queries[s:s + chunk], self.data_, h, out_scale=norm, log_eps=0.0, out=out[s:s + chunk])
+            # exact log-density also where the FP32 sum underflows (far queries)
+            ops.kde16_sum(queries[s:s + chunk], self.data_, h, out_scale=norm, log_exact=True,
+                          out=out[s:s + chunk])
         return out
 
     def _radius2(self, x: torch.Tensor) -> torch.Tensor:

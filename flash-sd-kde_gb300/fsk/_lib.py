@@ -28,6 +28,7 @@ FSK_LAPLACE = 0x2
 FSK_OUT_LOG = 0x4
 FSK_ATOMIC = 0x8
 FSK_WEIGHTED_FEATURE_MAJOR = 0x10
+FSK_OUT_LOG_EXACT = 0x20
 
 FSK_SCORE_ORDERED = 0
 FSK_SCORE_SYMMETRIC = 1

@@ -79,9 +79,15 @@ def kde16_sum(
     atomic: bool = False,
     out_scale: float = 1.0,
     log_eps: float | None = None,
+    log_exact: bool = False,
     out: torch.Tensor | None = None,
 ) -> torch.Tensor:
-    """out[i] = out_scale * sum_j phi(q_i, x_j)  (or log(out_scale*sum + log_eps))."""
+    """out[i] = out_scale * sum_j phi(q_i, x_j)  (or log(out_scale*sum + log_eps)).
+
+    log_exact: out[i] = log(out_scale * sum) without the eps floor and without
+    underflow (queries whose sum underflows are recomputed with a
+    running-minimum shift); needs log_eps None or 0.
+    """
     h = _check_bw(bandwidth)
     dev = _device(queries.device)
     q = as_matrix(queries, dev)
@@ -91,6 +97,11 @@ def kde16_sum(
         raise ValueError("data and queries must contain at least one sample.")
     flags = (L.FSK_PREC_IEEE if precision == "ieee" else L.FSK_PREC_TENSOR)
     flags |= (L.FSK_LAPLACE if laplace else 0) | (L.FSK_ATOMIC if atomic else 0)
+    if log_exact:
+        if log_eps:
+            raise ValueError("log_exact takes no log_eps (the log is taken without a floor).")
+        log_eps = 0.0
+        flags |= L.FSK_OUT_LOG_EXACT
     if log_eps is not None:
         flags |= L.FSK_OUT_LOG
     lib = L.load()

@@ -60,10 +60,11 @@ enum fsk_status {
 
 /* ---- option flags ------------------------------------------------------ */
 /* precision_mode "fast_tf32" of the reference: tensor-core split-precision
- * distance products (fp16 hi/lo pairs, three products, FP32 accumulation,
- * norms folded into the accumulator) and an exact FP32 direct-difference
- * recompute of every pair that carries more than 1/64 of its query's running
- * sum.  This is the default (value 0). */
+ * distance products (centred, scaled coordinates as three fp16 parts
+ * hi + mid + lo, seven products, FP32 accumulation, norms folded into bias
+ * columns of the operands) and an exact FP32 direct-difference recompute of
+ * the largest pair of every 32-pair chunk that carries more than 1/8 of its
+ * query's running sum.  This is the default (value 0). */
 #define FSK_PREC_TENSOR 0x0
 /* precision_mode "fp32_ieee": every pair by FP32 direct differences on the
  * CUDA cores, no tensor cores. */
@@ -73,6 +74,15 @@ enum fsk_status {
 #define FSK_LAPLACE 0x2
 /* Write out = log(out_scale * sum + out_eps) instead of out_scale * sum. */
 #define FSK_OUT_LOG 0x4
+/* fsk_kde16 with FSK_OUT_LOG and out_eps = 0 (m < 2^32): out = log(out_scale
+ * * sum) without underflow.  No counterpart in the reference, whose estimator
+ * floors at log(density + 1e-12) (flash_sd_kde/estimator.py:114).  Queries
+ * whose sum is below n 2^-100 (where the terms FP32 flushes to zero could
+ * matter: farther than ~11 h from every data point) are recomputed by FP32
+ * direct differences with a running-minimum shift,
+ * sum_j exp(-(dist_j - dmin) / (2 h^2)), and get
+ * log(that) - dmin / (2 h^2) + log(out_scale) in FP64. */
+#define FSK_OUT_LOG_EXACT 0x20
 /* Reduce splits with FP64 atomics instead of the ordered partial buffer
  * (kde_backend="atomic" / emp_score_backend="symmetric_atomic"). */
 #define FSK_ATOMIC 0x8

@@ -61,6 +61,10 @@ def test_argument_validation_is_host_side(lib):
     assert lib.fsk_kde16(fake, 10, fake, 10, -1.0, 0, 1.0, 0.0, fake, fake, 1 << 20, None) == inval
     assert lib.fsk_kde16(fake, 10, fake, 10, float("inf"), 0, 1.0, 0.0, fake, fake, 1 << 20, None) == inval
     assert lib.fsk_kde16(fake, 10, fake, 10, 1.0, 0x1000, 1.0, 0.0, fake, fake, 1 << 20, None) == inval
+    # exact log output: needs FSK_OUT_LOG and out_eps = 0
+    assert lib.fsk_kde16(fake, 10, fake, 10, 1.0, L.FSK_OUT_LOG_EXACT, 1.0, 0.0, fake, fake, 1 << 20, None) == inval
+    assert lib.fsk_kde16(fake, 10, fake, 10, 1.0, L.FSK_OUT_LOG_EXACT | L.FSK_OUT_LOG, 1.0, 1e-12, fake, fake,
+                         1 << 20, None) == inval
     assert lib.fsk_empscore16(fake, 10, 1.0, 7, 0, fake, fake, fake, 1 << 20, None) == inval
     assert lib.fsk_silverman(fake, 10, 65, 0, fake, fake, 1 << 20, None) == inval
     assert lib.fsk_silverman(fake, 10, 2, 1, fake, fake, 1 << 20, None) == inval
@@ -76,6 +80,12 @@ def test_argument_validation_is_host_side(lib):
 
 
 def test_workspace_sizes(lib):
+    from fsk import _lib as L
+
+    # the exact log output adds its list and per-part (dmin, sum) rows: >= 100 B per query
+    plain = lib.fsk_kde16_workspace_bytes(1 << 16, 1 << 16, L.FSK_OUT_LOG)
+    exact = lib.fsk_kde16_workspace_bytes(1 << 16, 1 << 16, L.FSK_OUT_LOG | L.FSK_OUT_LOG_EXACT)
+    assert exact >= plain + 100 * (1 << 16)
     a = lib.fsk_kde16_workspace_bytes(1 << 10, 1 << 12, 0)
     b = lib.fsk_kde16_workspace_bytes(1 << 20, 1 << 20, 0)
     assert 0 < a < b

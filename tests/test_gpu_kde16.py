@@ -181,3 +181,95 @@ def test_bounded_wait_timeout_is_reported(cuda_dev):
     ops.device_status(cuda_dev)          # cleared
     x = torch.randn(64, 16, device=cuda_dev)
     assert torch.isfinite(ops.kde16_sum(x, x, 1.0)).all()
+
+
+# ---- exact log-densities (FSK_OUT_LOG_EXACT) ---------------------------------
+
+def _far_case(seed, n=3000, m_near=300, m_far=300):
+    """N(0, I) data; queries in support and 5-40 standard deviations away
+    (every FP32 term of the far queries underflows)."""
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal((n, 16)).astype(np.float32)
+    near = rng.standard_normal((m_near, 16)).astype(np.float32)
+    direc = rng.standard_normal((m_far, 16))
+    direc /= np.linalg.norm(direc, axis=1, keepdims=True)
+    radius = rng.uniform(5.0, 40.0, (m_far, 1))
+    far = (direc * radius + 0.3 * rng.standard_normal((m_far, 16))).astype(np.float32)
+    q = np.concatenate([near, far])
+    q = q[rng.permutation(q.shape[0])]
+    return x, q, float(R.silverman_bandwidth_nd(x))
+
+
+def _log_exact(dev, q, x, h, precision="tensor"):
+    from fsk import ops
+
+    norm = 1.0 / ((2.0 * np.pi) ** 8 * h ** 16 * x.shape[0])
+    out = ops.kde16_sum(torch.from_numpy(q).to(dev), torch.from_numpy(x).to(dev), h, precision=precision,
+                        out_scale=norm, log_exact=True)
+    ops.device_status(dev)
+    return out.cpu().numpy().astype(np.float64)
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_log_exact_far_queries(cuda_dev, precision):
+    """log-densities of in-support and far queries vs the FP64 oracle:
+    |error| <= 1e-5 + 2e-6 |log p| (FP32 squared distances of far queries carry
+    ~1e-7 relative rounding, i.e. ~1e-4 absolute in log p at 30 h)."""
+    x, q, h = _far_case(0)
+    out = _log_exact(cuda_dev, q, x, h, precision)
+    ref = fp64.log_density(x, q, h)
+    assert np.isfinite(out).all()
+    assert ref.min() < -1000.0          # far queries underflow FP32 by hundreds of nats
+    err = np.abs(out - ref)
+    assert (err <= 1e-5 + 2e-6 * np.abs(ref)).all(), float((err / (1e-5 + 2e-6 * np.abs(ref))).max())
+    assert (err / np.abs(ref)).max() < 1e-6
+
+
+def test_log_exact_matches_plain_log_in_support(cuda_dev):
+    """Queries whose sum does not underflow take the plain path: bitwise the
+    value of FSK_OUT_LOG with eps = 0."""
+    from fsk import ops
+
+    x, q, h = _far_case(1, m_far=0)
+    norm = 1.0 / ((2.0 * np.pi) ** 8 * h ** 16 * x.shape[0])
+    qd, xd = torch.from_numpy(q).to(cuda_dev), torch.from_numpy(x).to(cuda_dev)
+    plain = ops.kde16_sum(qd, xd, h, out_scale=norm, log_eps=0.0).cpu().numpy()
+    exact = ops.kde16_sum(qd, xd, h, out_scale=norm, log_exact=True).cpu().numpy()
+    ops.device_status(cuda_dev)
+    assert np.array_equal(plain, exact)
+
+
+@pytest.mark.parametrize("n,m", [(1, 1), (33, 5), (31, 200), (4097, 1)])
+def test_log_exact_all_far_ragged(cuda_dev, n, m):
+    """Every query far away (all recomputed), ragged data tiles; two runs are
+    bitwise identical although the recompute list order may differ."""
+    rng = np.random.default_rng(n * 7 + m)
+    x = rng.standard_normal((n, 16)).astype(np.float32)
+    q = (rng.standard_normal((m, 16)) + 12.0).astype(np.float32)
+    h = 0.5
+    a = _log_exact(cuda_dev, q, x, h)
+    b = _log_exact(cuda_dev, q, x, h)
+    ref = fp64.log_density(x, q, h)
+    assert np.array_equal(a, b)
+    assert (np.abs(a - ref) <= 1e-5 + 2e-6 * np.abs(ref)).all()
+
+
+def test_kde_eval_log_eps0_and_estimator_log_space(cuda_dev):
+    """kde_eval_log(eps=0) and FlashSDKDE(log_space=True) return the exact
+    log-density; the default estimator keeps the reference's log(p + eps)
+    floor for far queries."""
+    from flash_sd_kde import FlashSDKDE
+    from flash_sd_kde.kde import kde_eval_log
+
+    x, q, h = _far_case(2, n=2000, m_near=100, m_far=100)
+    ref = fp64.log_density(x, q, h)
+    tol = 1e-5 + 2e-6 * np.abs(ref)
+    out = kde_eval_log(torch.from_numpy(x).to(cuda_dev), torch.from_numpy(q).to(cuda_dev), h, eps=0.0,
+                       device=cuda_dev).cpu().numpy()
+    assert (np.abs(out - ref) <= tol).all()
+    est = FlashSDKDE(bandwidth=h, mode="kde", device=cuda_dev, log_space=True).fit(x)
+    assert (np.abs(est.score_samples(q) - ref) <= tol).all()
+    floor = FlashSDKDE(bandwidth=h, mode="kde", device=cuda_dev).fit(x).score_samples(q)
+    far = ref < -200.0
+    assert far.any() and np.allclose(floor[far], np.log(1e-12), rtol=0, atol=1e-5)
+
