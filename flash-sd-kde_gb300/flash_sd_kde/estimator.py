@@ -30,7 +30,9 @@ class FlashSDKDE:
     - ``fit(X)`` stores train data (or SD-debiased train data for ``mode="sd_kde"``).
     - ``score_samples(X)`` returns log density values for each query sample.
     - ``score(X)`` returns the average log density.
-    ``mode="sd_kde"`` requires 16-D inputs; ``mode="kde"`` accepts 1-D or 16-D.
+    Inputs may have 1 to 16 features in both modes (an addition: the
+    reference requires 16 for ``mode="sd_kde"`` and 1 or 16 for ``mode="kde"``);
+    fewer than 16 are zero-padded, which leaves every distance unchanged.
     """
 
     bandwidth: BandwidthSpec = "silverman"
@@ -63,14 +65,16 @@ class FlashSDKDE:
         self.bandwidth_ = self._resolve_bandwidth(x_dev)
         self.X_fit_ = x_fit
         if self.mode == "sd_kde":
-            if self.n_features_in_ != ND_FEATURES:
+            if self.n_features_in_ > ND_FEATURES:
                 raise ValueError(
-                    f'mode="sd_kde" currently requires {ND_FEATURES} features, but got {self.n_features_in_}.'
+                    f'mode="sd_kde" supports at most {ND_FEATURES} features (fewer are zero-padded), '
+                    f'but got {self.n_features_in_}.'
                 )
-            self._fit_eval_data = emp_sd_kde_fit_transform(
+            deb = emp_sd_kde_fit_transform(
                 x_dev, self.bandwidth_, device=dev, precision_mode=self.precision_mode,
                 emp_score_backend=self.emp_score_backend, use_precomputed_norms=self.use_precomputed_norms,
                 autotune=self.autotune, eps=self.eps)
+            self._fit_eval_data = deb[:, 0].contiguous() if self.n_features_in_ == 1 else deb
         else:
             self._fit_eval_data = x_dev[:, 0].contiguous() if self.n_features_in_ == 1 else x_dev
         self._is_fitted = True

@@ -4,6 +4,10 @@ kde_eval                      route by ndim and backend, normalise   (reference 
 kde_eval_linearized           Laplace-corrected KDE, fused           (reference :127-149)
 kde_eval_linearized_nonfused  same quantity (see its docstring)      (reference :152-255)
 emp_sd_kde_fit_transform      score backends + debias shift          (reference :258-326)
+
+2-D inputs may have any 1 <= d <= 16 features (an addition: the reference
+requires exactly 16): rows are zero-padded to 16, which leaves every squared
+distance unchanged, and the normalisation uses d.
 """
 from __future__ import annotations
 
@@ -81,12 +85,16 @@ def _kde_eval_impl(data, queries, bandwidth, *, device, precision_mode, kde_back
         return ops.kde1d_sum(query, train, bandwidth, laplace=apply_laplacian_correction, atomic=atomic,
                              out_scale=scale, log_eps=log_eps)
     if ndim == 2:
-        train = ops.as_matrix(data, device, ND_FEATURES)
-        query = ops.as_matrix(queries, device, ND_FEATURES)
+        train, d = ops.as_padded_matrix(data, device, ND_FEATURES)
+        query, dq = ops.as_padded_matrix(queries, device, ND_FEATURES)
+        if dq != d:
+            raise ValueError(f"data has {d} features but queries have {dq}.")
+        if apply_laplacian_correction and d != ND_FEATURES:
+            raise ValueError(f"the Laplace-corrected KDE expects 1-D or {ND_FEATURES}-D data, got {d} features.")
         n_data = train.shape[0]
         if n_data == 0 or query.shape[0] == 0:
             raise ValueError("data and queries must be non-empty.")
-        norm = 1.0 / ((2.0 * math.pi) ** (ND_FEATURES / 2.0) * (bandwidth ** ND_FEATURES) * n_data)
+        norm = 1.0 / ((2.0 * math.pi) ** (d / 2.0) * (bandwidth ** d) * n_data)
         prec = "ieee" if precision_mode == PRECISION_FP32_IEEE else "tensor"
         return ops.kde16_sum(query, train, bandwidth, precision=prec, laplace=apply_laplacian_correction,
                              atomic=atomic, out_scale=norm, log_eps=None if log_exact else log_eps,
@@ -187,7 +195,7 @@ def emp_sd_kde_fit_transform(
         emp_score_backend = select_emp_score_backend(_n_rows(data), heuristics=DEFAULT_HEURISTICS)
     validate_emp_score_backend(emp_score_backend)
     device = _require_cuda(device, "emp_sd_kde_fit_transform")
-    train = ops.as_matrix(data, device, ND_FEATURES)
+    train, d = ops.as_padded_matrix(data, device, ND_FEATURES)
     if train.shape[0] == 0:
         raise ValueError("data must be non-empty.")
     prec = "ieee" if precision_mode == PRECISION_FP32_IEEE else "tensor"
@@ -199,5 +207,8 @@ def emp_sd_kde_fit_transform(
             feature_major=emp_score_backend == EMP_SCORE_BACKEND_FLASH_SD_KDE)
     if return_debug:
         debiased, score = ops.debias16(train, pdf_sum, weighted_sum, bandwidth, eps, return_score=True)
+        if d < ND_FEATURES:   # the padded columns are 0 in every output
+            return debiased[:, :d].contiguous(), pdf_sum, weighted_sum[:, :d], score[:, :d].contiguous()
         return debiased, pdf_sum, weighted_sum, score
-    return ops.debias16(train, pdf_sum, weighted_sum, bandwidth, eps)
+    debiased = ops.debias16(train, pdf_sum, weighted_sum, bandwidth, eps)
+    return debiased[:, :d].contiguous() if d < ND_FEATURES else debiased

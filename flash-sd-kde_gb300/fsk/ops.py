@@ -40,6 +40,24 @@ def as_matrix(x: Sequence[Sequence[float]] | torch.Tensor, device: torch.device,
     return t.contiguous()
 
 
+def as_padded_matrix(x: Sequence[Sequence[float]] | torch.Tensor, device: torch.device,
+                     width: int = ND_FEATURES) -> tuple[torch.Tensor, int]:
+    """(n, d) rows with 1 <= d <= width as a contiguous (n, width) FP32 tensor,
+    zero-padded, and d.  Zero coordinates add nothing to any squared distance,
+    so every pairwise Gaussian sum (and weighted sum, in the first d columns)
+    of the padded rows equals that of the original rows."""
+    if isinstance(x, torch.Tensor):
+        t = x.to(device=device, dtype=torch.float32, copy=False)
+    else:
+        t = torch.as_tensor(x, dtype=torch.float32, device=device)
+    if t.ndim != 2 or not 1 <= t.shape[1] <= width:
+        raise ValueError(f"expected tensor with shape (n, d), 1 <= d <= {width}, got {tuple(t.shape)}")
+    d = int(t.shape[1])
+    if d < width:
+        t = torch.nn.functional.pad(t, (0, width - d))
+    return t.contiguous(), d
+
+
 def as_vector(x: Sequence[float] | torch.Tensor, device: torch.device) -> torch.Tensor:
     if isinstance(x, torch.Tensor):
         t = x.to(device=device, dtype=torch.float32, copy=False)

@@ -61,6 +61,24 @@ def test_estimator_input_validation():
         est.score_samples(np.zeros((3, 16), np.float32))
 
 
+def test_padded_rows():
+    """1 <= d <= 16 features are zero-padded to 16 (distances unchanged); more are rejected."""
+    import torch
+
+    from fsk import ops
+
+    cpu = torch.device("cpu")
+    x = np.arange(15, dtype=np.float32).reshape(3, 5)
+    t, d = ops.as_padded_matrix(x, cpu)
+    assert d == 5 and t.shape == (3, 16) and t.is_contiguous()
+    assert np.array_equal(t[:, :5].numpy(), x) and not t[:, 5:].any()
+    t16, d16 = ops.as_padded_matrix(np.ones((2, 16), np.float32), cpu)
+    assert d16 == 16 and t16.shape == (2, 16)
+    for bad in (np.zeros((3, 17), np.float32), np.zeros((3, 0), np.float32), np.zeros(4, np.float32)):
+        with pytest.raises(ValueError):
+            ops.as_padded_matrix(bad, cpu)
+
+
 def test_kernel_wrappers_reject_bad_arguments():
     from kernels.flash_sd_kde import gaussian_kde_triton_nd, emp_score_16d_flash_sd_kde
     from kernels.kde_eval_16d_stream_splitk import kde_eval_16d_splitk
