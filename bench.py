@@ -72,7 +72,7 @@ def parse():
     ap.add_argument("--sur-train", type=int, default=262144, help="surrogate workload: exact SD-KDE fit points")
     ap.add_argument("--sur-pairs", type=int, default=4_000_000, help="surrogate workload: training pairs")
     ap.add_argument("--sur-eval", type=int, default=1_000_000, help="surrogate workload: held-out queries")
-    ap.add_argument("--op", choices=["kde16", "kde16_logexact", "score16"], default=None,
+    ap.add_argument("--op", choices=["kde16", "kde16_logexact", "score16", "kde1d"], default=None,
                     help="time one operation alone on n GMM8 points (profiling case; no contract line)")
     ap.add_argument("--n", type=int, default=N_TRAIN, help="points for --op (queries = data)")
     return ap.parse_args()
@@ -511,7 +511,10 @@ def run_op(args) -> None:
     points as data and as queries, Silverman bandwidth, W warm-up and K timed
     launches with CUDA events on the launching stream.  kde16_logexact: exact
     log-densities with half the queries moved 60 bandwidths away from the data
-    (every term of those underflows FP32, so they take the shifted recompute)."""
+    (every term of those underflows FP32, so they take the shifted recompute).
+    kde1d: 4 n points of the 1-D three-component mixture against n grid
+    queries on [-5, 6] (the large 1-D configuration at n = 2^20)."""
+    import numpy as np
     import torch
 
     import __graft_entry__ as ge
@@ -520,6 +523,17 @@ def run_op(args) -> None:
     from fsk import ops, workloads
 
     dev = torch.device("cuda", 0)
+    if args.op == "kde1d":
+        rng = np.random.default_rng(1)
+        comp = rng.choice(3, size=4 * args.n, p=[0.3, 0.5, 0.2])
+        x1 = (np.array([-2.0, 0.0, 3.0])[comp] + np.array([0.5, 1.0, 0.3])[comp] *
+              rng.standard_normal(4 * args.n)).astype(np.float32)
+        xd = torch.from_numpy(x1).to(dev)
+        qd = torch.linspace(-5.0, 6.0, args.n, device=dev)
+        h1 = float(fp_sdkde_1d(x1))
+        fn = lambda: ops.kde1d_sum(qd, xd, h1)
+        pairs = float(args.n) * 4 * args.n
+        return _time_op(args, dev, fn, pairs, h1)
     x = torch.from_numpy(workloads.GMM16(seed=0).sample(args.n, seed=1)).to(dev)
     h = float(ops.silverman(x).item())
     if args.op == "kde16":
@@ -530,6 +544,23 @@ def run_op(args) -> None:
         fn = lambda: ops.kde16_sum(q, x, h, log_exact=True)
     else:
         fn = lambda: ops.empscore16(x, h)
+    _time_op(args, dev, fn, float(args.n) * args.n, h)
+
+
+def fp_sdkde_1d(x) -> float:
+    """Silverman-type 1-D bandwidth 0.9 min(std, IQR/1.34) n^(-1/5) in FP64 (host)."""
+    import numpy as np
+
+    x = np.asarray(x, np.float64)
+    iqr = np.percentile(x, 75) - np.percentile(x, 25)
+    return 0.9 * min(x.std(), iqr / 1.34) * x.size ** (-0.2)
+
+
+def _time_op(args, dev, fn, pairs, h) -> None:
+    import torch
+
+    from fsk import ops
+
     for _ in range(args.warmup):
         fn()
     torch.cuda.synchronize(dev)
@@ -543,7 +574,7 @@ def run_op(args) -> None:
     ops.device_status(dev)
     ms = s_ev.elapsed_time(e_ev) / args.steps
     print(json.dumps({"op": args.op, "n": args.n, "h": h, "ms_per_call": ms,
-                      "pair_evals_per_s": float(args.n) * args.n / (ms * 1e-3)}), flush=True)
+                      "pair_evals_per_s": pairs / (ms * 1e-3)}), flush=True)
 
 
 def main():

@@ -339,13 +339,38 @@ int64_t sym_simt_pairs(int64_t n) {
 }
 
 // ---------------------------------------------------------------------------
-// 1-D KDE.  Block 128 threads x Q1 queries; data tiles of T1 points in SMEM.
+// 1-D KDE.  Block 128 threads x K1_Q queries; data tiles of K1_T points in SMEM.
 // phi = exp(-(q - x)^2 / (2 h^2)) (times 1.5 - (q-x)^2/(2h^2) with Laplace).
+// A thread's queries are held negated in f32x2 pairs, so one packed
+// instruction forms x - q, its square and the exponent for two queries: the
+// FP32 work per pair drops below the ex2 rate and the exp pipe is the bound.
+// Per query the arithmetic (x - q = -(q - x) exactly, squared, times
+// -log2(e)/(2h^2), ex2, summed in data order) is that of a scalar loop.
 // ---------------------------------------------------------------------------
 namespace {
 constexpr int K1_THREADS = 128;
 constexpr int K1_Q = 8;
+constexpr int K1_P = K1_Q / 2;   // query pairs per thread
 constexpr int K1_T = 1024;
+
+// Visits the valid points r0 .. rend-1 of a staged tile in order: four at a
+// time (one 16-byte shared load) for a full 32-point group, else one by one.
+template <typename F>
+__device__ __forceinline__ void for_points(const float* xs, int r0, int rend, F&& f) {
+  if (rend - r0 == 32) {
+    const float4* xs4 = reinterpret_cast<const float4*>(xs + r0);
+#pragma unroll 2
+    for (int k = 0; k < 8; ++k) {
+      const float4 v = xs4[k];
+      f(v.x);
+      f(v.y);
+      f(v.z);
+      f(v.w);
+    }
+  } else {
+    for (int r = r0; r < rend; ++r) f(xs[r]);
+  }
+}
 }  // namespace
 
 template <bool LAPLACE>
@@ -354,15 +379,18 @@ __global__ void __launch_bounds__(K1_THREADS) kde1d_kernel(
     float c1, int64_t tiles_per_split, double* __restrict__ partials, double* __restrict__ atomic_acc) {
   __shared__ __align__(16) float xs[K1_T];
   const int64_t q0 = (int64_t)blockIdx.x * (K1_THREADS * K1_Q);
-  float qr[K1_Q];
+  float2 nq[K1_P];   // -q of queries (2p, 2p + 1)
 #pragma unroll
-  for (int u = 0; u < K1_Q; ++u) {
-    int64_t qi = q0 + threadIdx.x + u * K1_THREADS;
-    qr[u] = qi < m ? q[qi] : 0.f;
+  for (int p = 0; p < K1_P; ++p) {
+    const int64_t qa = q0 + threadIdx.x + (2 * p) * K1_THREADS, qb = qa + K1_THREADS;
+    nq[p] = make_float2(qa < m ? -q[qa] : 0.f, qb < m ? -q[qb] : 0.f);
   }
   Comp acc[K1_Q];
 #pragma unroll
   for (int u = 0; u < K1_Q; ++u) acc[u] = Comp{0.f, 0.f};
+  const float2 nc2_2 = make_float2(nc2, nc2);
+  const float2 mc1_2 = make_float2(-c1, -c1);
+  const float2 c15_2 = make_float2(1.5f, 1.5f);
   const int64_t n_tiles = (n + K1_T - 1) / K1_T;
   const int64_t t_begin = (int64_t)blockIdx.y * tiles_per_split;
   const int64_t t_end = min(n_tiles, t_begin + tiles_per_split);
@@ -373,23 +401,26 @@ __global__ void __launch_bounds__(K1_THREADS) kde1d_kernel(
     for (int e = threadIdx.x; e < K1_T; e += K1_THREADS) xs[e] = e < valid ? x[j0 + e] : 0.f;
     __syncthreads();
     for (int r0 = 0; r0 < valid; r0 += 32) {
-      float part[K1_Q];
+      float2 part[K1_P];
 #pragma unroll
-      for (int u = 0; u < K1_Q; ++u) part[u] = 0.f;
-      const int rend = min(valid, r0 + 32);
-      for (int r = r0; r < rend; ++r) {
-        const float xv = xs[r];
+      for (int p = 0; p < K1_P; ++p) part[p] = make_float2(0.f, 0.f);
+      for_points(xs, r0, min(valid, r0 + 32), [&](float xv) {
+        const float2 x2 = make_float2(xv, xv);
 #pragma unroll
-        for (int u = 0; u < K1_Q; ++u) {
-          float d = qr[u] - xv;
-          float t2 = d * d;
-          float e = ex2_approx(t2 * nc2);
-          if (LAPLACE) e *= fmaf(-c1, t2, 1.5f);
-          part[u] += e;
+        for (int p = 0; p < K1_P; ++p) {
+          const float2 d = __fadd2_rn(x2, nq[p]);
+          const float2 t2 = __fmul2_rn(d, d);
+          const float2 a = __fmul2_rn(t2, nc2_2);
+          float2 e = make_float2(ex2_approx(a.x), ex2_approx(a.y));
+          if (LAPLACE) e = __fmul2_rn(e, __ffma2_rn(mc1_2, t2, c15_2));
+          part[p] = __fadd2_rn(part[p], e);
         }
-      }
+      });
 #pragma unroll
-      for (int u = 0; u < K1_Q; ++u) acc[u].add(part[u]);
+      for (int p = 0; p < K1_P; ++p) {
+        acc[2 * p].add(part[p].x);
+        acc[2 * p + 1].add(part[p].y);
+      }
     }
   }
 #pragma unroll
@@ -431,12 +462,13 @@ __global__ void __launch_bounds__(K1_THREADS) kde1d_score_kernel(
     int64_t tiles_per_split, double* __restrict__ p0, double* __restrict__ p1) {
   __shared__ __align__(16) float xs[K1_T];
   const int64_t q0 = (int64_t)blockIdx.x * (K1_THREADS * K1_Q);
-  float qr[K1_Q];
+  float2 nq[K1_P];   // -q of queries (2p, 2p + 1)
 #pragma unroll
-  for (int u = 0; u < K1_Q; ++u) {
-    int64_t qi = q0 + threadIdx.x + u * K1_THREADS;
-    qr[u] = qi < m ? q[qi] : 0.f;
+  for (int p = 0; p < K1_P; ++p) {
+    const int64_t qa = q0 + threadIdx.x + (2 * p) * K1_THREADS, qb = qa + K1_THREADS;
+    nq[p] = make_float2(qa < m ? -q[qa] : 0.f, qb < m ? -q[qb] : 0.f);
   }
+  const float2 nc2_2 = make_float2(nc2, nc2);
   Comp a0[K1_Q], a1[K1_Q];
 #pragma unroll
   for (int u = 0; u < K1_Q; ++u) { a0[u] = Comp{0.f, 0.f}; a1[u] = Comp{0.f, 0.f}; }
@@ -450,22 +482,27 @@ __global__ void __launch_bounds__(K1_THREADS) kde1d_score_kernel(
     for (int e = threadIdx.x; e < K1_T; e += K1_THREADS) xs[e] = e < valid ? x[j0 + e] : 0.f;
     __syncthreads();
     for (int r0 = 0; r0 < valid; r0 += 32) {
-      float s0[K1_Q], s1[K1_Q];
+      float2 s0[K1_P], s1[K1_P];
 #pragma unroll
-      for (int u = 0; u < K1_Q; ++u) { s0[u] = 0.f; s1[u] = 0.f; }
-      const int rend = min(valid, r0 + 32);
-      for (int r = r0; r < rend; ++r) {
-        const float xv = xs[r];
+      for (int p = 0; p < K1_P; ++p) { s0[p] = make_float2(0.f, 0.f); s1[p] = make_float2(0.f, 0.f); }
+      for_points(xs, r0, min(valid, r0 + 32), [&](float xv) {
+        const float2 x2 = make_float2(xv, xv);
 #pragma unroll
-        for (int u = 0; u < K1_Q; ++u) {
-          float d = qr[u] - xv;
-          float e = ex2_approx(d * d * nc2);
-          s0[u] += e;
-          s1[u] = fmaf(-d, e, s1[u]);
+        for (int p = 0; p < K1_P; ++p) {
+          const float2 d = __fadd2_rn(x2, nq[p]);    // x - q
+          const float2 a = __fmul2_rn(__fmul2_rn(d, d), nc2_2);
+          const float2 e = make_float2(ex2_approx(a.x), ex2_approx(a.y));
+          s0[p] = __fadd2_rn(s0[p], e);
+          s1[p] = __ffma2_rn(d, e, s1[p]);
         }
-      }
+      });
 #pragma unroll
-      for (int u = 0; u < K1_Q; ++u) { a0[u].add(s0[u]); a1[u].add(s1[u]); }
+      for (int p = 0; p < K1_P; ++p) {
+        a0[2 * p].add(s0[p].x);
+        a0[2 * p + 1].add(s0[p].y);
+        a1[2 * p].add(s1[p].x);
+        a1[2 * p + 1].add(s1[p].y);
+      }
     }
   }
 #pragma unroll
