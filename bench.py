@@ -54,9 +54,11 @@ KERNEL_NAMES = {1: "kde16_tc_kernel", 2: "kde16_simt_kernel", 3: "score16_simt_k
                 7: "score16_tc_kernel"}
 # fp16 tensor-core flops per pair evaluation issued by the tcgen05 kernels:
 # KDE: 7 MMAs (M=128, N=128, K=16; three-part operands) per 128x128 pairs;
-# score: 4 MMAs (M=128, N=64, K=16; two-part operands) per 128x64 pairs plus
-# 16 MMAs (M=128, N=32, K=16) per 256x64 pairs for the weighted sum.
-MMA_FLOPS_PER_PAIR = {"kde16_tc_kernel": 7 * 2 * 16, "score16_tc_kernel": 4 * 2 * 16 + 16 * 2 * 128 * 32 * 16 / (256 * 64)}
+# score: 7 MMAs (M=128, N=64, K=16; three-part operands) per 128x64 pairs plus,
+# per 128x64 pairs, 4 MMAs of N=32 (hi weights x [X_hi | X_lo]) and 4 of N=16
+# (lo weights x X_hi), K=16, for the weighted sum.
+MMA_FLOPS_PER_PAIR = {"kde16_tc_kernel": 7 * 2 * 16,
+                      "score16_tc_kernel": 7 * 2 * 16 + 2 * 128 * 16 * (4 * 32 + 4 * 16) / (128 * 64)}
 
 
 def parse():

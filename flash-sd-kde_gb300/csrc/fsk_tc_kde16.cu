@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
           tc_fence_after();
           const uint64_t so = (uint64_t)(s * (KB_STAGE_BYTES >> 4));
           if (lane == 0) {
-            mma_s_tile<true>(d0 + b * (uint32_t)(NQT * KNT), a_h, a_m, a_l, b_h0 + so, b_m0 + so, b_l0 + so, idesc);
+            mma_s_tile(d0 + b * (uint32_t)(NQT * KNT), a_h, a_m, a_l, b_h0 + so, b_m0 + so, b_l0 + so, idesc);
             mma_commit(&tfull[b * NQT + a]);
             mma_commit(&empty[s]);
           }

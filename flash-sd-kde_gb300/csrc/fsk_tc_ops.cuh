@@ -26,21 +26,14 @@ __device__ __forceinline__ void mma_f16_ss(uint32_t d_tmem, uint64_t a_desc, uin
 // D = a2 for one 128-query tile x one data tile (smallest products first, so
 // the large hi.hi and bias terms meet last, then the bias K step).
 // a_h / b_h: H images (hi | bias), a_m / b_m: mid, a_l / b_l: lo images.
-// THREE_PART: the six products whose error terms exceed ~2^-33 (seven MMAs);
-// otherwise the two-part product hi.hi + hi.mid + mid.hi (four MMAs, error
-// terms ~2^-22), for kernels whose tensor pipe is the tighter resource.
-template <bool THREE_PART>
+// The six products whose error terms exceed ~2^-33, then the bias: seven MMAs.
 __device__ __forceinline__ void mma_s_tile(uint32_t d, uint64_t a_h, uint64_t a_m, uint64_t a_l, uint64_t b_h,
                                            uint64_t b_m, uint64_t b_l, uint32_t idesc) {
   const uint64_t bias = 256 >> 4;   // bias K step: +256 B in the start-address field
-  if (THREE_PART) {
-    mma_f16_ss(d, a_m, b_m, idesc, 0u);     // mid . mid
-    mma_f16_ss(d, a_h, b_l, idesc, 1u);     // hi . lo
-    mma_f16_ss(d, a_l, b_h, idesc, 1u);     // lo . hi
-    mma_f16_ss(d, a_h, b_m, idesc, 1u);     // hi . mid
-  } else {
-    mma_f16_ss(d, a_h, b_m, idesc, 0u);     // hi . mid
-  }
+  mma_f16_ss(d, a_m, b_m, idesc, 0u);       // mid . mid
+  mma_f16_ss(d, a_h, b_l, idesc, 1u);       // hi . lo
+  mma_f16_ss(d, a_l, b_h, idesc, 1u);       // lo . hi
+  mma_f16_ss(d, a_h, b_m, idesc, 1u);       // hi . mid
   mma_f16_ss(d, a_m, b_h, idesc, 1u);       // mid . hi
   mma_f16_ss(d, a_h, b_h, idesc, 1u);       // hi . hi
   mma_f16_ss(d, a_h + bias, b_h + bias, idesc, 1u);   // beta_j + alpha_i

@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
         const uint64_t so = (uint64_t)((s * S_STAGE_BYTES) >> 4);
         const uint32_t d = tmem_base + (uint32_t)(T_S + b * (SNQT * NT) + a * NT);
         const uint64_t b_h = dh0 + so;
-        // three-part product, small terms first (the order of mma_s_tile<true>)
+        // three-part product, small terms first (the order of mma_s_tile)
         const uint64_t b_m = dm0 + so, b_l = dl0 + so;
         if (lane == 0) {
           mma_f16_ts(d, a_h + 16u, b_m, idesc_s, 0u);                    // mid . mid
