@@ -255,6 +255,74 @@ int fsk_debias16(const float* data, int64_t n, const float* pdf_sum, const float
   return cuda_status(cudaGetLastError());
 }
 
+// ---- any d <= FSK_ND_MAX (CUDA cores) ------------------------------------------------
+size_t fsk_kde_nd_workspace_bytes(int64_t m, int64_t n, int d, int flags) {
+  (void)flags;
+  if (m < 1 || n < 1 || d < 1 || d > FSK_ND_MAX) return 0;
+  return align_up((size_t)kde_nd_splits(m, n, d) * m * sizeof(double), 256);
+}
+
+int fsk_kde_nd(const float* queries, int64_t m, const float* data, int64_t n, int d, double bandwidth, int flags,
+               double out_scale, double out_eps, float* out, void* workspace, size_t workspace_bytes, void* stream) {
+  if (!queries || !data || !out || m < 1 || n < 1 || d < 1 || d > FSK_ND_MAX || bad_bw(bandwidth))
+    return FSK_ERR_INVALID_ARGUMENT;
+  if (flags & ~(FSK_PREC_IEEE | FSK_LAPLACE | FSK_OUT_LOG | FSK_ATOMIC)) return FSK_ERR_INVALID_ARGUMENT;
+  int st = check_device();
+  if (st) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!workspace || workspace_bytes < fsk_kde_nd_workspace_bytes(m, n, d, flags)) return FSK_ERR_WORKSPACE_TOO_SMALL;
+  const int splits = kde_nd_splits(m, n, d);
+  double* part = static_cast<double*>(workspace);
+  launch_kde_nd(queries, m, data, n, d, bandwidth, (flags & FSK_LAPLACE) != 0, splits, part, s);
+  launch_reduce_rows(part, splits, m, out_scale, out_eps, (flags & FSK_OUT_LOG) != 0, out, s);
+  return cuda_status(cudaGetLastError());
+}
+
+static size_t empscore_nd_bytes(int64_t n, int d) {
+  WsCarver c(nullptr, 0);
+  const int splits = score_nd_splits(n);
+  c.take<double>((size_t)FSK_ND_MAX);
+  c.take<float>((size_t)FSK_ND_MAX);
+  c.take<double>((size_t)splits * n);
+  c.take<double>((size_t)splits * n * d);
+  return align_up(c.used, 256);
+}
+
+size_t fsk_empscore_nd_workspace_bytes(int64_t n, int d) {
+  if (n < 1 || d < 1 || d > FSK_ND_MAX) return 0;
+  return empscore_nd_bytes(n, d);
+}
+
+int fsk_empscore_nd(const float* data, int64_t n, int d, double bandwidth, float* pdf_sum, float* weighted_sum,
+                    void* workspace, size_t workspace_bytes, void* stream) {
+  if (!data || !pdf_sum || !weighted_sum || n < 1 || d < 1 || d > FSK_ND_MAX || bad_bw(bandwidth))
+    return FSK_ERR_INVALID_ARGUMENT;
+  int st = check_device();
+  if (st) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!workspace || workspace_bytes < empscore_nd_bytes(n, d)) return FSK_ERR_WORKSPACE_TOO_SMALL;
+  WsCarver c(workspace, workspace_bytes);
+  const int splits = score_nd_splits(n);
+  double* mu64 = c.take<double>((size_t)FSK_ND_MAX);
+  float* mu = c.take<float>((size_t)FSK_ND_MAX);
+  double* ppdf = c.take<double>((size_t)splits * n);
+  double* pw = c.take<double>((size_t)splits * n * d);
+  launch_score_nd(data, n, d, bandwidth, splits, mu64, mu, ppdf, pw, pdf_sum, weighted_sum, s);
+  return cuda_status(cudaGetLastError());
+}
+
+int fsk_debias_nd(const float* data, int64_t n, int d, const float* pdf_sum, const float* weighted_sum,
+                  double bandwidth, double eps, float* debiased, float* score, void* stream) {
+  if (!data || !pdf_sum || !weighted_sum || !debiased || n < 1 || d < 1 || d > FSK_ND_MAX || bad_bw(bandwidth) ||
+      !(eps >= 0.0))
+    return FSK_ERR_INVALID_ARGUMENT;
+  int st = check_device();
+  if (st) return st;
+  launch_debias_nd(data, n, d, pdf_sum, weighted_sum, bandwidth, eps, debiased, score,
+                   static_cast<cudaStream_t>(stream));
+  return cuda_status(cudaGetLastError());
+}
+
 // ---- 1-D ------------------------------------------------------------------------
 size_t fsk_kde1d_workspace_bytes(int64_t m, int64_t n, int flags) {
   if (m < 1 || n < 1) return 0;

@@ -42,6 +42,8 @@ enum KernelId {
   K_SCORE16_TC = 7,
   K_MLP_INFER = 9,   // work unit: one (query, ensemble member) evaluation
   K_KDE16_LOGSPACE = 10,   // shifted recompute of underflowing queries (work not known on the host)
+  K_KDE_ND = 11,
+  K_SCORE_ND = 12,
 };
 
 // RAII bracket of one kernel launch with CUDA events on its stream when the

@@ -62,6 +62,18 @@ void launch_reduce_logexact(const float* q, int64_t m, const float* x, int64_t n
                             const double* partials, int splits, double scale, const LogExactBufs& b, float* out,
                             cudaStream_t s);
 
+// ---- fsk_nd.cu ------------------------------------------------------------------
+// any 1 <= d <= FSK_ND_MAX features, rows with stride d (CUDA cores)
+int kde_nd_splits(int64_t m, int64_t n, int d);
+int score_nd_splits(int64_t n);
+void launch_kde_nd(const float* q, int64_t m, const float* x, int64_t n, int d, double h, bool laplace, int splits,
+                   double* partials, cudaStream_t s);
+// mu64/mu: FSK_ND_MAX entries; ppdf [splits][n], pw [splits][n][d]; writes pdf (n) and w (n, d)
+void launch_score_nd(const float* x, int64_t n, int d, double h, int splits, double* mu64, float* mu, double* ppdf,
+                     double* pw, float* pdf, float* w, cudaStream_t s);
+void launch_debias_nd(const float* x, int64_t n, int d, const float* pdf, const float* w, double h, double eps,
+                      float* deb, float* score, cudaStream_t s);
+
 // ---- fsk_silverman.cu -----------------------------------------------------------
 size_t silverman_ws_bytes(int64_t n, int d);
 int run_silverman(const float* x, int64_t n, int d, int rule, double* h_out, void* ws, size_t ws_bytes,

@@ -17,7 +17,8 @@ import torch
 
 from flash_sd_kde.kde import _kde_eval_impl, emp_sd_kde_fit_transform
 from fsk import ops
-from globals import DEFAULT_EPS, DEFAULT_KDE_BACKEND, DEFAULT_PRECISION_MODE, ND_FEATURES
+from fsk._lib import FSK_ND_MAX
+from globals import DEFAULT_EPS, DEFAULT_KDE_BACKEND, DEFAULT_PRECISION_MODE
 
 FlashMode = Literal["sd_kde", "kde"]
 BandwidthSpec = float | Literal["silverman"]
@@ -30,9 +31,10 @@ class FlashSDKDE:
     - ``fit(X)`` stores train data (or SD-debiased train data for ``mode="sd_kde"``).
     - ``score_samples(X)`` returns log density values for each query sample.
     - ``score(X)`` returns the average log density.
-    Inputs may have 1 to 16 features in both modes (an addition: the
+    Inputs may have 1 to 64 features in both modes (an addition: the
     reference requires 16 for ``mode="sd_kde"`` and 1 or 16 for ``mode="kde"``);
-    fewer than 16 are zero-padded, which leaves every distance unchanged.
+    fewer than 16 are zero-padded, which leaves every distance unchanged, and
+    more than 16 run on the CUDA-core kernels for any d.
     """
 
     bandwidth: BandwidthSpec = "silverman"
@@ -65,10 +67,9 @@ class FlashSDKDE:
         self.bandwidth_ = self._resolve_bandwidth(x_dev)
         self.X_fit_ = x_fit
         if self.mode == "sd_kde":
-            if self.n_features_in_ > ND_FEATURES:
+            if self.n_features_in_ > FSK_ND_MAX:
                 raise ValueError(
-                    f'mode="sd_kde" supports at most {ND_FEATURES} features (fewer are zero-padded), '
-                    f'but got {self.n_features_in_}.'
+                    f'mode="sd_kde" supports at most {FSK_ND_MAX} features, but got {self.n_features_in_}.'
                 )
             deb = emp_sd_kde_fit_transform(
                 x_dev, self.bandwidth_, device=dev, precision_mode=self.precision_mode,

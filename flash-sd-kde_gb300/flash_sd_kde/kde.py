@@ -5,9 +5,11 @@ kde_eval_linearized           Laplace-corrected KDE, fused           (reference 
 kde_eval_linearized_nonfused  same quantity (see its docstring)      (reference :152-255)
 emp_sd_kde_fit_transform      score backends + debias shift          (reference :258-326)
 
-2-D inputs may have any 1 <= d <= 16 features (an addition: the reference
-requires exactly 16): rows are zero-padded to 16, which leaves every squared
-distance unchanged, and the normalisation uses d.
+2-D inputs may have any 1 <= d <= 64 features (an addition: the reference
+requires exactly 16).  Up to 16 the rows are zero-padded to 16 (which leaves
+every squared distance unchanged) and take the 16-D kernels; above 16 the
+CUDA-core kernels for any d (fp32_ieee arithmetic) run.  The normalisation
+uses d.
 """
 from __future__ import annotations
 
@@ -51,6 +53,13 @@ def _infer_ndim(data) -> int:
     return 1
 
 
+def _n_features(data) -> int:
+    """Columns of 2-D input (0 when it has no second axis)."""
+    if isinstance(data, (torch.Tensor, np.ndarray)):
+        return int(data.shape[1]) if data.ndim == 2 else 0
+    return len(data[0]) if len(data) and isinstance(data[0], (list, tuple, np.ndarray)) else 0
+
+
 def _n_rows(data) -> int:
     return data.shape[0] if isinstance(data, (torch.Tensor, np.ndarray)) else len(data)
 
@@ -85,12 +94,24 @@ def _kde_eval_impl(data, queries, bandwidth, *, device, precision_mode, kde_back
         return ops.kde1d_sum(query, train, bandwidth, laplace=apply_laplacian_correction, atomic=atomic,
                              out_scale=scale, log_eps=log_eps)
     if ndim == 2:
+        d = _n_features(data)
+        # more than 16 features, or the Laplace factor 1 + d/2 - dist/(2h^2)
+        # for d != 16 (the 16-D kernels build in d = 16): CUDA-core kernels for any d
+        if d > ND_FEATURES or (apply_laplacian_correction and d != ND_FEATURES):
+            if log_exact:
+                raise ValueError(f"exact log-densities are available for up to {ND_FEATURES} features.")
+            train, query = ops._as_rows(data, device), ops._as_rows(queries, device)
+            if query.shape[1] != d:
+                raise ValueError(f"data has {d} features but queries have {query.shape[1]}.")
+            if train.shape[0] == 0 or query.shape[0] == 0:
+                raise ValueError("data and queries must be non-empty.")
+            norm = 1.0 / ((2.0 * math.pi) ** (d / 2.0) * (bandwidth ** d) * train.shape[0])
+            return ops.kde_nd_sum(query, train, bandwidth, laplace=apply_laplacian_correction, out_scale=norm,
+                                  log_eps=log_eps)
         train, d = ops.as_padded_matrix(data, device, ND_FEATURES)
         query, dq = ops.as_padded_matrix(queries, device, ND_FEATURES)
         if dq != d:
             raise ValueError(f"data has {d} features but queries have {dq}.")
-        if apply_laplacian_correction and d != ND_FEATURES:
-            raise ValueError(f"the Laplace-corrected KDE expects 1-D or {ND_FEATURES}-D data, got {d} features.")
         n_data = train.shape[0]
         if n_data == 0 or query.shape[0] == 0:
             raise ValueError("data and queries must be non-empty.")
@@ -195,6 +216,15 @@ def emp_sd_kde_fit_transform(
         emp_score_backend = select_emp_score_backend(_n_rows(data), heuristics=DEFAULT_HEURISTICS)
     validate_emp_score_backend(emp_score_backend)
     device = _require_cuda(device, "emp_sd_kde_fit_transform")
+    if _n_features(data) > ND_FEATURES:
+        train = ops._as_rows(data, device)
+        if train.shape[0] == 0:
+            raise ValueError("data must be non-empty.")
+        pdf_sum, weighted_sum = ops.empscore_nd(train, bandwidth)
+        if return_debug:
+            debiased, score = ops.debias_nd(train, pdf_sum, weighted_sum, bandwidth, eps, return_score=True)
+            return debiased, pdf_sum, weighted_sum, score
+        return ops.debias_nd(train, pdf_sum, weighted_sum, bandwidth, eps)
     train, d = ops.as_padded_matrix(data, device, ND_FEATURES)
     if train.shape[0] == 0:
         raise ValueError("data must be non-empty.")

@@ -30,6 +30,8 @@ FSK_ATOMIC = 0x8
 FSK_WEIGHTED_FEATURE_MAJOR = 0x10
 FSK_OUT_LOG_EXACT = 0x20
 
+FSK_ND_MAX = 64
+
 FSK_SCORE_ORDERED = 0
 FSK_SCORE_SYMMETRIC = 1
 
@@ -52,6 +54,11 @@ SIGNATURES: dict[str, tuple] = {
     "fsk_kde16_workspace_bytes": (_sz, [_i64, _i64, _int]),
     "fsk_kde16": (_int, [_vp, _i64, _vp, _i64, _d, _int, _d, _d, _vp, _vp, _sz, _vp]),
     "fsk_kde16_noalloc": (_int, [_vp, _i64, _vp, _i64, _d, _int, _d, _d, _vp, _vp]),
+    "fsk_kde_nd_workspace_bytes": (_sz, [_i64, _i64, _int, _int]),
+    "fsk_kde_nd": (_int, [_vp, _i64, _vp, _i64, _int, _d, _int, _d, _d, _vp, _vp, _sz, _vp]),
+    "fsk_empscore_nd_workspace_bytes": (_sz, [_i64, _int]),
+    "fsk_empscore_nd": (_int, [_vp, _i64, _int, _d, _vp, _vp, _vp, _sz, _vp]),
+    "fsk_debias_nd": (_int, [_vp, _i64, _int, _vp, _vp, _d, _d, _vp, _vp, _vp]),
     "fsk_empscore16_workspace_bytes": (_sz, [_i64, _int, _int]),
     "fsk_empscore16": (_int, [_vp, _i64, _d, _int, _int, _vp, _vp, _vp, _sz, _vp]),
     "fsk_debias16": (_int, [_vp, _i64, _vp, _vp, _i64, _i64, _d, _d, _vp, _vp, _vp]),

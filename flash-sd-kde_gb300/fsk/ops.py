@@ -166,6 +166,77 @@ def empscore16(
     return pdf, (w.t() if feature_major else w)
 
 
+def _as_rows(x, device: torch.device) -> torch.Tensor:
+    t = x.to(device=device, dtype=torch.float32, copy=False) if isinstance(x, torch.Tensor) else \
+        torch.as_tensor(x, dtype=torch.float32, device=device)
+    if t.ndim != 2 or not 1 <= t.shape[1] <= L.FSK_ND_MAX:
+        raise ValueError(f"expected tensor with shape (n, d), 1 <= d <= {L.FSK_ND_MAX}, got {tuple(t.shape)}")
+    return t.contiguous()
+
+
+def kde_nd_sum(queries, data, bandwidth: float, *, laplace: bool = False, out_scale: float = 1.0,
+               log_eps: float | None = None) -> torch.Tensor:
+    """out[i] = out_scale * sum_j phi(q_i, x_j) (or log(out_scale*sum + log_eps))
+    for rows of any 1 <= d <= 64 features (CUDA-core kernel, fp32_ieee arithmetic)."""
+    h = _check_bw(bandwidth)
+    dev = _device(data.device if isinstance(data, torch.Tensor) else "cuda")
+    q, x = _as_rows(queries, dev), _as_rows(data, dev)
+    m, n, d = q.shape[0], x.shape[0], x.shape[1]
+    if q.shape[1] != d:
+        raise ValueError(f"data has {d} features but queries have {q.shape[1]}.")
+    if m == 0 or n == 0:
+        raise ValueError("data and queries must contain at least one sample.")
+    flags = (L.FSK_LAPLACE if laplace else 0) | (L.FSK_OUT_LOG if log_eps is not None else 0)
+    lib = L.load()
+    with torch.cuda.device(dev):
+        out = torch.empty(m, dtype=torch.float32, device=dev)
+        ws = _workspace(lib.fsk_kde_nd_workspace_bytes(m, n, d, flags), dev)
+        st = lib.fsk_kde_nd(q.data_ptr(), m, x.data_ptr(), n, d, h, flags, float(out_scale), float(log_eps or 0.0),
+                            out.data_ptr(), ws.data_ptr(), ws.numel(), _stream(dev))
+    L.check(st, "fsk_kde_nd")
+    return out
+
+
+def empscore_nd(data, bandwidth: float) -> tuple[torch.Tensor, torch.Tensor]:
+    """(pdf_sum (n,), weighted_sum (n, d)) for rows of any 1 <= d <= 64 features."""
+    h = _check_bw(bandwidth)
+    dev = _device(data.device if isinstance(data, torch.Tensor) else "cuda")
+    x = _as_rows(data, dev)
+    n, d = x.shape
+    if n == 0:
+        raise ValueError("data must contain at least one element.")
+    lib = L.load()
+    with torch.cuda.device(dev):
+        pdf = torch.empty(n, dtype=torch.float32, device=dev)
+        w = torch.empty((n, d), dtype=torch.float32, device=dev)
+        ws = _workspace(lib.fsk_empscore_nd_workspace_bytes(n, d), dev)
+        st = lib.fsk_empscore_nd(x.data_ptr(), n, d, h, pdf.data_ptr(), w.data_ptr(), ws.data_ptr(), ws.numel(),
+                                 _stream(dev))
+    L.check(st, "fsk_empscore_nd")
+    return pdf, w
+
+
+def debias_nd(data, pdf_sum: torch.Tensor, weighted_sum: torch.Tensor, bandwidth: float, eps: float, *,
+              return_score: bool = False):
+    """The debias shift of debias16 for rows of any 1 <= d <= 64 features."""
+    h = _check_bw(bandwidth)
+    dev = _device(data.device if isinstance(data, torch.Tensor) else "cuda")
+    x = _as_rows(data, dev)
+    n, d = x.shape
+    pdf = pdf_sum.to(device=dev, dtype=torch.float32).contiguous()
+    w = weighted_sum.to(device=dev, dtype=torch.float32).contiguous()
+    if w.shape != (n, d) or pdf.shape != (n,):
+        raise ValueError("pdf_sum must be (n,) and weighted_sum (n, d).")
+    lib = L.load()
+    with torch.cuda.device(dev):
+        deb = torch.empty_like(x)
+        score = torch.empty_like(x) if return_score else None
+        st = lib.fsk_debias_nd(x.data_ptr(), n, d, pdf.data_ptr(), w.data_ptr(), h, float(eps), deb.data_ptr(),
+                               _ptr(score), _stream(dev))
+    L.check(st, "fsk_debias_nd")
+    return (deb, score) if return_score else deb
+
+
 def debias16(
     data: torch.Tensor,
     pdf_sum: torch.Tensor,

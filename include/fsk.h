@@ -124,6 +124,29 @@ FSK_API int fsk_kde16_noalloc(const float* queries, int64_t m, const float* data
                               double bandwidth, int flags, double out_scale, double out_eps,
                               float* out, void* stream);
 
+/* ---- any feature count 1 <= d <= FSK_ND_MAX (CUDA cores) ---------------- */
+/* No counterpart in the reference snapshot, which fixes d = 16
+ * (ND_FEATURES, globals.py:25; its paper's review answers describe padding
+ * to a multiple of 16).  Rows (n, d) / (m, d) row-major FP32 with stride d;
+ * the "fp32_ieee" arithmetic of the 16-D CUDA-core kernels: FP32 direct
+ * differences, compensated FP32 sums per split, fixed-order FP64 reduction.
+ * fsk_kde_nd: out as fsk_kde16 (flags FSK_LAPLACE with the factor
+ * 1 + d/2 - dist/(2 h^2), FSK_OUT_LOG; FSK_PREC_IEEE and FSK_ATOMIC are
+ * accepted and change nothing).  fsk_empscore_nd: pdf_sum (n) and
+ * weighted_sum (n, d) row-major, self pair included.  fsk_debias_nd: the
+ * shift of fsk_debias16 for (n, d) rows; score may be NULL. */
+#define FSK_ND_MAX 64
+FSK_API size_t fsk_kde_nd_workspace_bytes(int64_t m, int64_t n, int d, int flags);
+FSK_API int fsk_kde_nd(const float* queries, int64_t m, const float* data, int64_t n, int d,
+                       double bandwidth, int flags, double out_scale, double out_eps, float* out,
+                       void* workspace, size_t workspace_bytes, void* stream);
+FSK_API size_t fsk_empscore_nd_workspace_bytes(int64_t n, int d);
+FSK_API int fsk_empscore_nd(const float* data, int64_t n, int d, double bandwidth, float* pdf_sum,
+                            float* weighted_sum, void* workspace, size_t workspace_bytes, void* stream);
+FSK_API int fsk_debias_nd(const float* data, int64_t n, int d, const float* pdf_sum,
+                          const float* weighted_sum, double bandwidth, double eps, float* debiased,
+                          float* score, void* stream);
+
 /* ---- 16-D empirical-score accumulators --------------------------------- */
 /* pdf_sum[i] = sum_j phi_ij, weighted_sum[i,:] = sum_j phi_ij x_j, the
  * self-pair included (flash_sd_kde/reference.py:263-284). */

@@ -62,8 +62,8 @@ def test_errors(cuda_dev):
 
     with pytest.raises(ValueError):
         FlashSDKDE().score_samples(np.zeros((3, 16), np.float32))
-    with pytest.raises(ValueError):   # at most 16 features (fewer are zero-padded)
-        FlashSDKDE(mode="sd_kde").fit(np.zeros((10, 17), np.float32))
+    with pytest.raises(ValueError):   # at most 64 features
+        FlashSDKDE(mode="sd_kde").fit(np.zeros((10, 65), np.float32))
     with pytest.raises(ValueError):
         FlashSDKDE(mode="bogus").fit(np.zeros((10, 16), np.float32))
     est = FlashSDKDE(mode="kde", bandwidth=1.0).fit(np.zeros((10, 16), np.float32))

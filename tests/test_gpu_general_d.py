@@ -1,7 +1,9 @@
-"""Feature counts 1 <= d <= 16 through the public API (zero-padded to 16 on
-the device) against the FP64 oracle: KDE in both precision modes, the SD-KDE
-debias shift and the estimator end to end.  Tolerances as for 16-D: densities
-1e-5 relative, debiased points 1e-5 relative with a 1e-5 * max|x| floor."""
+"""Feature counts other than 16 through the public API against the FP64
+oracle: 1 <= d <= 16 zero-padded to 16 on the device (tensor-core kernels),
+16 < d <= 64 on the CUDA-core kernels for any d; KDE in both precision modes,
+the Laplace-corrected KDE, the SD-KDE debias shift and the estimator end to
+end.  Tolerances as for 16-D: densities 1e-5 relative, debiased points 1e-5
+relative with a 1e-5 * max|x| floor."""
 import numpy as np
 import pytest
 import torch
@@ -64,15 +66,62 @@ def test_estimator_general_d(cuda_dev, mode):
     assert (np.abs(out - ref) / np.abs(ref)).max() < 1e-5
 
 
+@pytest.mark.parametrize("d", [17, 40, 64])
+def test_kde_eval_above_16(cuda_dev, d):
+    """d > 16: the CUDA-core kernels for any d (both precision modes take them)."""
+    from flash_sd_kde import kde_eval
+
+    x, q = _data(d, 2000, 300, d)
+    h = fp64.silverman_nd(x)
+    truth = np.exp(fp64.log_density(x, q, h))
+    for precision in ("fast_tf32", "fp32_ieee"):
+        out = kde_eval(torch.from_numpy(x).to(cuda_dev), torch.from_numpy(q).to(cuda_dev), h, device=cuda_dev,
+                       precision_mode=precision).cpu().numpy()
+        assert rel_err(out, truth).max() < 1e-5, (precision, rel_err(out, truth).max())
+
+
+@pytest.mark.parametrize("d", [5, 33])
+def test_laplace_general_d(cuda_dev, d):
+    """Laplace-corrected KDE with the factor 1 + d/2 - dist/(2h^2) of the data's d."""
+    from flash_sd_kde import kde_eval_linearized
+
+    x, q = _data(d, 1500, 200, 3 + d)
+    h = 1.5 * fp64.silverman_nd(x)
+    out = kde_eval_linearized(torch.from_numpy(x).to(cuda_dev), torch.from_numpy(q).to(cuda_dev), h,
+                              device=cuda_dev).cpu().numpy().astype(np.float64)
+    truth = np.exp(fp64.log_density(x, q, h, laplace=True))   # |sum phi (1 + d/2 - dist/(2h^2))| / norm
+    big = np.abs(out) > 1e-3 * np.abs(out).max()             # the corrected sum cancels elsewhere
+    assert rel_err(np.abs(out[big]), truth[big]).max() < 1e-4
+
+
+def test_sd_kde_above_16(cuda_dev):
+    from flash_sd_kde import FlashSDKDE, emp_sd_kde_fit_transform
+
+    x, q = _data(24, 1500, 200, 24)
+    h = fp64.silverman_nd(x)
+    deb, pdf, w, score = emp_sd_kde_fit_transform(torch.from_numpy(x).to(cuda_dev), h, device=cuda_dev,
+                                                  return_debug=True)
+    p64, w64, _ = fp64.empirical_score(x, h)
+    assert deb.shape == (1500, 24) and w.shape == (1500, 24)
+    np.testing.assert_allclose(pdf.cpu().numpy(), p64, rtol=1e-5)
+    np.testing.assert_allclose(w.cpu().numpy(), w64, rtol=1e-5, atol=1e-5 * np.abs(w64).max())
+    d64 = fp64.debias(x, h)
+    np.testing.assert_allclose(deb.cpu().numpy(), d64, rtol=1e-5, atol=1e-5 * np.abs(d64).max())
+    est = FlashSDKDE(mode="sd_kde", bandwidth=h, device=cuda_dev).fit(x)
+    ref = np.log(np.exp(fp64.log_density(d64, q, h)) + est.eps)
+    assert (np.abs(est.score_samples(q) - ref) / np.abs(ref)).max() < 1e-5
+
+
 def test_general_d_argument_errors(cuda_dev):
-    from flash_sd_kde import FlashSDKDE, kde_eval, kde_eval_linearized
+    from flash_sd_kde import FlashSDKDE, kde_eval
+    from flash_sd_kde.kde import kde_eval_log
 
     x5 = np.zeros((10, 5), np.float32)
     with pytest.raises(ValueError):
         kde_eval(x5, np.zeros((3, 6), np.float32), 1.0, device=cuda_dev)
     with pytest.raises(ValueError):
-        kde_eval_linearized(x5, x5, 1.0, device=cuda_dev)
+        kde_eval(np.zeros((10, 65), np.float32), np.zeros((3, 65), np.float32), 1.0, device=cuda_dev)
+    with pytest.raises(ValueError):   # exact log output: up to 16 features
+        kde_eval_log(np.zeros((10, 20), np.float32), np.zeros((3, 20), np.float32), 1.0, eps=0.0, device=cuda_dev)
     with pytest.raises(ValueError):
-        kde_eval(np.zeros((10, 17), np.float32), np.zeros((3, 17), np.float32), 1.0, device=cuda_dev)
-    with pytest.raises(ValueError):
-        FlashSDKDE(mode="sd_kde", device=cuda_dev).fit(np.random.default_rng(0).standard_normal((50, 20)))
+        FlashSDKDE(mode="sd_kde", device=cuda_dev).fit(np.random.default_rng(0).standard_normal((50, 65)))
