@@ -119,14 +119,18 @@ struct ScParams {
   double* pw;     // [splits][n][16]  centred weighted sums, self pair excluded
 };
 
-// f32 pair -> packed fp16 hi and lo parts (hi + lo = v to ~22 bits)
+// f32 pair -> packed fp16 hi and lo parts (hi + lo = v to ~22 bits).  The
+// residual v - hi is exact in FP32 (hi holds v's leading 11 bits) and comes
+// from one mixed-precision FMA per value, fp16 hi times -1 plus the FP32 v.
 __device__ __forceinline__ void split_pack(float v0, float v1, uint32_t& hi, uint32_t& lo) {
-  const __half2 h = __floats2half2_rn(v0, v1);
-  const float2 hf = __half22float2(h);
-  const float2 r = __fadd2_rn(make_float2(v0, v1), make_float2(-hf.x, -hf.y));
-  const __half2 l = __floats2half2_rn(r.x, r.y);
-  hi = *reinterpret_cast<const uint32_t*>(&h);
-  lo = *reinterpret_cast<const uint32_t*>(&l);
+  asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(hi) : "f"(v1), "f"(v0));
+  float r0, r1;
+  const unsigned short minus_one = 0xBC00;   // fp16 -1
+  asm("{\n\t.reg .b16 h0, h1;\n\tmov.b32 {h0, h1}, %2;\n\t"
+      "fma.rn.f32.f16 %0, h0, %5, %3;\n\tfma.rn.f32.f16 %1, h1, %5, %4;\n\t}"
+      : "=f"(r0), "=f"(r1)
+      : "r"(hi), "f"(v0), "f"(v1), "h"(minus_one));
+  asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(lo) : "f"(r1), "f"(r0));
 }
 
 // Walks the (unit, data tile) sequence of one CTA: units are (query block,
