@@ -48,7 +48,10 @@ constexpr int MMA_ISSUERS = 2;
 constexpr int THREADS = (EPI_WARPS + 3) * 32;
 constexpr int TMEM_COLS = 2 * NQT * KNT; // double-buffered accumulators
 constexpr int K_BAR_OFFSET = A_BYTES + NS * KB_STAGE_BYTES;
-constexpr int SMEM_BYTES = K_BAR_OFFSET + 256;
+// KDE: one 64-byte slot per epilogue thread for its query's FP32 row (read by
+// the exact recompute; each thread writes its own slot at the start of a unit)
+constexpr int K_QX_OFFSET = K_BAR_OFFSET + 256;
+constexpr int SMEM_BYTES = K_QX_OFFSET + EPI_WARPS * 32 * FSK_D * 4;
 // A term is recomputed exactly when its 32-column chunk holds more than this
 // fraction of the running sum of its query (the chunk included).  With the
 // three-part operands the exponent of any other term is off by at most

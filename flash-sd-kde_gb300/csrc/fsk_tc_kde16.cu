@@ -196,6 +196,7 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
     const uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
     const float out_mul = p.scales->out_mul;
     const bool scaled = out_mul != 1.0f;
+    float4* qslot = reinterpret_cast<float4*>(smem_raw + K_QX_OFFSET) + (warp * 32 + lane) * (FSK_D / 4);
     uint32_t g = 0;
     int s = 0;
     int64_t prev_qb = -1;
@@ -207,7 +208,13 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
         prev_qb = qb;
       }
       const int64_t gi = qb * (NQT * QT) + qt * QT + quarter * 32 + lane;   // padded query index
-      const float* qrow = p.qexact + gi * FSK_D;   // read only by the (rare) exact recompute
+      // this query's FP32 row into the thread's own shared-memory slot (read
+      // only by the exact recompute; the slot is rewritten only by this thread)
+      {
+        const float4* src = reinterpret_cast<const float4*>(p.qexact + gi * FSK_D);
+#pragma unroll
+        for (int kk = 0; kk < FSK_D / 4; ++kk) qslot[kk] = src[kk];
+      }
       Comp acc{0.f, 0.f};
       float corr = 0.f;
       const int64_t t0 = sp * p.tiles_per_split;
@@ -316,7 +323,7 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
                 float qx[FSK_D];
 #pragma unroll
                 for (int kk = 0; kk < FSK_D; kk += 4) {
-                  const float4 v = *reinterpret_cast<const float4*>(qrow + kk);
+                  const float4 v = qslot[kk / 4];
                   qx[kk] = v.x; qx[kk + 1] = v.y; qx[kk + 2] = v.z; qx[kk + 3] = v.w;
                 }
                 const float dist = exact_dist(xrows, c * 32 + j, qx, 0);
