@@ -107,6 +107,9 @@ def workload_config() -> dict:
 # ---------------------------------------------------------------------------
 # CPU baseline / reference arm
 # ---------------------------------------------------------------------------
+REFERENCE_ARM_SECONDS = 90.0   # CPU work of the reference arm's timed steps, all together
+
+
 def cpu_baseline(target_seconds: float, steps: int = 1) -> dict:
     cmd = [sys.executable, "-m", "oracle.cpu_baseline", "--n", str(N_TRAIN),
            "--target-seconds", str(target_seconds), "--steps", str(steps)]
@@ -122,8 +125,11 @@ def run_reference_arm(args) -> None:
     if rank != 0:
         return
     warm = cpu_baseline(2.0, steps=max(1, min(args.warmup, 1)))
+    # the whole timed run is held to ~90 s of CPU work whatever --steps is:
+    # each step is a sample of (at least 128) rows sized to 90 s / steps
+    per_step = max(0.05, min(6.0, REFERENCE_ARM_SECONDS / max(1, args.steps)))
     t0 = time.perf_counter()
-    res = cpu_baseline(6.0, steps=args.steps)
+    res = cpu_baseline(per_step, steps=args.steps)
     wall = time.perf_counter() - t0
     pairs_step = res["value"] * res["seconds"] / args.steps
     line = {
