@@ -66,6 +66,16 @@ def test_argument_validation_is_host_side(lib):
     assert lib.fsk_kde16(fake, 10, fake, 10, 1.0, L.FSK_OUT_LOG_EXACT | L.FSK_OUT_LOG, 1.0, 1e-12, fake, fake,
                          1 << 20, None) == inval
     assert lib.fsk_empscore16(fake, 10, 1.0, 7, 0, fake, fake, fake, 1 << 20, None) == inval
+    # any-d entry points: 1 <= d <= FSK_ND_MAX, known flags, eps >= 0
+    for d in (0, L.FSK_ND_MAX + 1):
+        assert lib.fsk_kde_nd(fake, 10, fake, 10, d, 1.0, 0, 1.0, 0.0, fake, fake, 1 << 20, None) == inval
+        assert lib.fsk_empscore_nd(fake, 10, d, 1.0, fake, fake, fake, 1 << 20, None) == inval
+        assert lib.fsk_debias_nd(fake, 10, d, fake, fake, 1.0, 0.0, fake, None, None) == inval
+        assert lib.fsk_kde_nd_workspace_bytes(10, 10, d, 0) == 0
+        assert lib.fsk_empscore_nd_workspace_bytes(10, d) == 0
+    assert lib.fsk_kde_nd(fake, 10, fake, 10, 20, 1.0, L.FSK_OUT_LOG_EXACT, 1.0, 0.0, fake, fake, 1 << 20,
+                          None) == inval
+    assert lib.fsk_debias_nd(fake, 10, 20, fake, fake, 1.0, -1.0, fake, None, None) == inval
     assert lib.fsk_silverman(fake, 10, 65, 0, fake, fake, 1 << 20, None) == inval
     assert lib.fsk_silverman(fake, 10, 2, 1, fake, fake, 1 << 20, None) == inval
     assert lib.fsk_kde1d(fake, 10, fake, 0, 1.0, 0, 1.0, 0.0, fake, fake, 1 << 20, None) == inval
