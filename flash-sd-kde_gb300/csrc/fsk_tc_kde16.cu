@@ -196,7 +196,9 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
     const uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
     const float out_mul = p.scales->out_mul;
     const bool scaled = out_mul != 1.0f;
-    float4* qslot = reinterpret_cast<float4*>(smem_raw + K_QX_OFFSET) + (warp * 32 + lane) * (FSK_D / 4);
+    // slot float4 kk of thread t at [kk][t]: a warp's 16-byte accesses are contiguous
+    float4* qslot = reinterpret_cast<float4*>(smem_raw + K_QX_OFFSET) + (warp * 32 + lane);
+    constexpr int QS_STRIDE = EPI_WARPS * 32;
     uint32_t g = 0;
     int s = 0;
     int64_t prev_qb = -1;
@@ -213,7 +215,7 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
       {
         const float4* src = reinterpret_cast<const float4*>(p.qexact + gi * FSK_D);
 #pragma unroll
-        for (int kk = 0; kk < FSK_D / 4; ++kk) qslot[kk] = src[kk];
+        for (int kk = 0; kk < FSK_D / 4; ++kk) qslot[kk * QS_STRIDE] = src[kk];
       }
       Comp acc{0.f, 0.f};
       float corr = 0.f;
@@ -323,7 +325,7 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
                 float qx[FSK_D];
 #pragma unroll
                 for (int kk = 0; kk < FSK_D; kk += 4) {
-                  const float4 v = qslot[kk / 4];
+                  const float4 v = qslot[(kk / 4) * QS_STRIDE];
                   qx[kk] = v.x; qx[kk + 1] = v.y; qx[kk + 2] = v.z; qx[kk + 3] = v.w;
                 }
                 const float dist = exact_dist(xrows, c * 32 + j, qx, 0);
