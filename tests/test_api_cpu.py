@@ -45,6 +45,23 @@ def test_kde_eval_rejects_bad_arguments_before_device_work():
         emp_sd_kde_fit_transform(x, 1.0, device="cpu")
 
 
+def test_log_and_feature_count_arguments_before_device_work():
+    """Host-side checks of the additions: exact log output needs eps >= 0,
+    the padded rows take 1 <= d <= 16, the any-d rows 1 <= d <= 64."""
+    import torch
+
+    from flash_sd_kde.kde import kde_eval_log
+    from fsk import ops
+
+    x = np.zeros((8, 16), np.float32)
+    with pytest.raises(ValueError):
+        kde_eval_log(x, x, 1.0, eps=-1.0)
+    with pytest.raises(ValueError):
+        ops._as_rows(np.zeros((4, 65), np.float32), torch.device("cpu"))
+    t = ops._as_rows(np.ones((4, 40), np.float32), torch.device("cpu"))
+    assert t.shape == (4, 40) and t.is_contiguous()
+
+
 def test_estimator_input_validation():
     from flash_sd_kde import FlashSDKDE
 
