@@ -125,3 +125,27 @@ def test_general_d_argument_errors(cuda_dev):
         kde_eval_log(np.zeros((10, 20), np.float32), np.zeros((3, 20), np.float32), 1.0, eps=0.0, device=cuda_dev)
     with pytest.raises(ValueError):
         FlashSDKDE(mode="sd_kde", device=cuda_dev).fit(np.random.default_rng(0).standard_normal((50, 65)))
+
+
+@pytest.mark.parametrize("d", [17, 64])
+@pytest.mark.parametrize("m,n", [(1, 1), (3, 33), (130, 31), (257, 65)])
+def test_any_d_ragged_shapes(cuda_dev, d, m, n):
+    """Any-d kernels at tiny and ragged sizes (partial 32-point tiles, one
+    query, one point): KDE, empirical score and debias vs FP64."""
+    from fsk import ops
+
+    rng = np.random.default_rng(d * 1000 + m * 7 + n)
+    x = rng.standard_normal((n, d)).astype(np.float32)
+    q = (x[rng.integers(0, n, m)] + 0.3 * rng.standard_normal((m, d))).astype(np.float32)
+    h = 1.2
+    out = ops.kde_nd_sum(torch.from_numpy(q).to(cuda_dev), torch.from_numpy(x).to(cuda_dev), h).cpu().numpy()
+    ref = np.exp(fp64.log_density(x, q, h)) * ((2.0 * np.pi) ** (d / 2.0) * h ** d * n)   # unnormalised sums
+    assert rel_err(out, ref).max() < 1e-5
+    pdf, w = ops.empscore_nd(torch.from_numpy(x).to(cuda_dev), h)
+    deb = ops.debias_nd(torch.from_numpy(x).to(cuda_dev), pdf, w, h, 1e-12)
+    ops.device_status(cuda_dev)
+    p64, w64, _ = fp64.empirical_score(x, h)
+    np.testing.assert_allclose(pdf.cpu().numpy(), p64, rtol=1e-5)
+    np.testing.assert_allclose(w.cpu().numpy(), w64, rtol=1e-5, atol=1e-5 * np.abs(w64).max())
+    d64 = fp64.debias(x, h)
+    np.testing.assert_allclose(deb.cpu().numpy(), d64, rtol=1e-5, atol=1e-5 * np.abs(d64).max())
