@@ -2,27 +2,33 @@
 """Benchmark of the Flash-SD-KDE hot path on GB300.
 
 Workload (one step): one-step empirical SD-KDE followed by KDE evaluation,
-d = 16, FP32 inputs: n_train = 65536 points from the 8-component Gaussian
-mixture (weights Dirichlet(1), means N(0, 4I), covariances A A^T/16 + 0.1 I)
-and 65536 fresh mixture queries; bandwidth by Silverman's rule.  A step is
+d = 16, FP32 inputs: n_train = n_query = 2^20 by default (--n) drawn from the
+8-component Gaussian mixture (weights Dirichlet(1), means N(0, 4I),
+covariances A A^T/16 + 0.1 I), the queries fresh draws; bandwidth by
+Silverman's rule.  A step is
   empirical score (pdf_sum, weighted_sum; n^2 pair evaluations)
-  + debias shift + KDE of the debiased set at the queries (n*m pairs).
-Metric: exact 16-D pair evaluations per second.
+  + debias shift + KDE of the debiased set at the queries (n*m pairs),
+through the public API (emp_sd_kde_fit_transform + kde_eval, default
+backends).  Metric: exact 16-D pair evaluations per second.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl fsk|reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl fsk|reference] [--n N]
 
 value      device-resident inputs, per-step CUDA events on the launching
            stream, L2 flushed (256 MiB write) before every timed step.
-e2e        the same step through the public API (emp_sd_kde_fit_transform +
-           kde_eval) from pinned host buffers, H2D and D2H inside the timing.
-roofline   the dominant kernel's pair-evals/s (library timer: CUDA events on
-           its own stream) against the exp-bound peak built from the SFU
+e2e        the same calls from pinned host buffers, the H2D copy of the
+           inputs and the D2H copy of the densities inside the timing.
+roofline   the dominant kernel's required exps/s (library timer: CUDA events
+           on its own stream) against the exp-bound peak built from the SFU
            ex2 and FP32 FMA rates measured on this GPU.
+triton_reference  the reference's own Triton kernels, unmodified, imported
+           from baseline/_ref in a child process, timed on the same GPU and
+           workload (paper protocol empirical_sd_kde_triton_nd +
+           gaussian_kde_triton_nd, and the default public API), with their
+           errors against FP64.
 cpu_baseline  the reference CPU path (numpy restatement) on a bounded
            sample with all host cores, in a subprocess.
 surrogate  the learned-surrogate workload (exact SD-KDE fit on 262144 points,
-           4 MLPs trained on 4M pairs, 1M held-out queries): gated,
-           surrogate-only and exact queries/s, served fraction, errors.
+           4 MLPs trained on 4M pairs, 1M held-out queries).
 Multi-GPU (torchrun): every rank runs an independent replica (own query
 set, shared training set); value = all ranks' pairs / max-over-ranks time.
 """
@@ -39,10 +45,11 @@ import time
 from pathlib import Path
 
 ROOT = Path(__file__).resolve().parent
-sys.path[:0] = [str(ROOT / "flash-sd-kde_gb300"), str(ROOT)]
+PKG = ROOT / "flash-sd-kde_gb300"
+REF_DIR = ROOT / "baseline" / "_ref"
+sys.path[:0] = [str(PKG), str(ROOT)]
 
-N_TRAIN = 65536
-N_QUERY = 65536
+N_DEFAULT = 1 << 20
 EPS = 1e-12
 # FP32-pipe lane operations per pair in the tensor-core KDE epilogue besides
 # the exp (scale-add, query offset, accumulate) and per polynomial exp2; used
@@ -51,32 +58,40 @@ C_OPS_PER_PAIR = 3.0
 K_OPS_PER_POLY_EXP = 10.0
 KERNEL_NAMES = {1: "kde16_tc_kernel", 2: "kde16_simt_kernel", 3: "score16_simt_kernel",
                 4: "score16_sym_simt_kernel", 5: "kde1d_kernel", 6: "kde1d_score_kernel",
-                7: "score16_tc_kernel"}
-# fp16 tensor-core flops per pair evaluation issued by the tcgen05 kernels:
-# KDE: 7 MMAs (M=128, N=128, K=16; three-part operands) per 128x128 pairs;
-# score: 7 MMAs (M=128, N=64, K=16; three-part operands) per 128x64 pairs plus,
-# per 128x64 pairs, 4 MMAs of N=32 (hi weights x [X_hi | X_lo]) and 4 of N=16
-# (lo weights x X_hi), K=16, for the weighted sum.
-MMA_FLOPS_PER_PAIR = {"kde16_tc_kernel": 7 * 2 * 16,
-                      "score16_tc_kernel": 7 * 2 * 16 + 2 * 128 * 16 * (4 * 32 + 4 * 16) / (128 * 64)}
+                7: "score16_tc_kernel", 8: "score16_sym_tc_kernel"}
+# Tensor-core flops per pair evaluation.  "issued": what the tcgen05 kernels
+# execute (three-part fp16 operands: seven K=16 MMAs for the exponent; the
+# score kernel's weighted sums as fp16 hi/lo weights times [X_hi | X_lo] and
+# X_hi).  "algorithmic": the contraction itself, 2*16 flops per pair for the
+# exponent's dot product, plus 2*16 for the weighted sum of the score.
+MMA_FLOPS_PER_PAIR = {"kde16_tc_kernel": {"issued": 7 * 2 * 16, "algorithmic": 2 * 16},
+                      "score16_tc_kernel": {"issued": 7 * 2 * 16 + 2 * 128 * 16 * (4 * 32 + 4 * 16) / (128 * 64),
+                                            "algorithmic": 2 * 2 * 16}}
 
 
 def parse():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["fsk", "reference"], default="fsk")
+    ap.add_argument("--n", type=int, default=N_DEFAULT, help="n_train = n_query of the SD-KDE workload")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-triton", action="store_true", help="leave the reference-Triton leg out")
+    ap.add_argument("--triton-leg", action="store_true", help=argparse.SUPPRESS)
+    ap.add_argument("--triton-steps", type=int, default=3)
+    ap.add_argument("--triton-ieee", action="store_true",
+                    help="also time the reference's fp32_ieee path (slow: CUDA-core FP32)")
+    ap.add_argument("--h", type=float, default=None, help=argparse.SUPPRESS)
     ap.add_argument("--surrogate", action="store_true",
                     help="run only the learned-surrogate workload (C4) and print its JSON line")
     ap.add_argument("--no-surrogate", action="store_true", help="leave the surrogate object out of the bench line")
     ap.add_argument("--sur-train", type=int, default=262144, help="surrogate workload: exact SD-KDE fit points")
     ap.add_argument("--sur-pairs", type=int, default=4_000_000, help="surrogate workload: training pairs")
     ap.add_argument("--sur-eval", type=int, default=1_000_000, help="surrogate workload: held-out queries")
-    ap.add_argument("--op", choices=["kde16", "kde16_logexact", "score16", "kde1d"], default=None,
+    ap.add_argument("--op", choices=["kde16", "kde16_logexact", "score16", "score16_sym", "kde1d", "precision"],
+                    default=None,
                     help="time one operation alone on n GMM8 points (profiling case; no contract line)")
-    ap.add_argument("--n", type=int, default=N_TRAIN, help="points for --op (queries = data)")
     return ap.parse_args()
 
 
@@ -91,17 +106,25 @@ def metric_name() -> str:
     return "16D pair-evals/s exact (SD-KDE: empirical score + debias + KDE)"
 
 
-def workload_config() -> dict:
+def workload_config(n: int) -> dict:
     return {
-        "workload": "sdkde_gmm8_16d_n65536_m65536",
-        "n_train": N_TRAIN,
-        "n_query": N_QUERY,
+        "workload": f"sdkde_gmm8_16d_n{n}_m{n}",
+        "n_train": n,
+        "n_query": n,
         "d": 16,
         "bandwidth": "silverman",
-        "pairs_per_step": N_TRAIN * N_TRAIN + N_TRAIN * N_QUERY,
+        "pairs_per_step": n * n + n * n,
+        "api": "flash_sd_kde.emp_sd_kde_fit_transform + flash_sd_kde.kde_eval (default backends)",
         "l2": "flushed before each timed step (256 MiB write)",
         "precision_mode": "fast_tf32 (three-part fp16 tensor-core exponents + exact FP32 near-pair recompute)",
     }
+
+
+def gmm_inputs(n: int, query_seed: int = 2):
+    from fsk import workloads
+
+    gmm = workloads.GMM16(seed=0)
+    return gmm.sample(n, seed=1), gmm.sample(n, seed=query_seed)
 
 
 # ---------------------------------------------------------------------------
@@ -110,8 +133,8 @@ def workload_config() -> dict:
 REFERENCE_ARM_SECONDS = 90.0   # CPU work of the reference arm's timed steps, all together
 
 
-def cpu_baseline(target_seconds: float, steps: int = 1) -> dict:
-    cmd = [sys.executable, "-m", "oracle.cpu_baseline", "--n", str(N_TRAIN),
+def cpu_baseline(n: int, target_seconds: float, steps: int = 1) -> dict:
+    cmd = [sys.executable, "-m", "oracle.cpu_baseline", "--n", str(n),
            "--target-seconds", str(target_seconds), "--steps", str(steps)]
     env = dict(os.environ, OMP_NUM_THREADS="1", OPENBLAS_NUM_THREADS="1", MKL_NUM_THREADS="1")
     res = subprocess.run(cmd, cwd=str(ROOT), capture_output=True, text=True, env=env, timeout=900)
@@ -124,12 +147,12 @@ def run_reference_arm(args) -> None:
     world, rank, _ = dist_env()
     if rank != 0:
         return
-    warm = cpu_baseline(2.0, steps=max(1, min(args.warmup, 1)))
+    warm = cpu_baseline(args.n, 2.0, steps=max(1, min(args.warmup, 1)))
     # the whole timed run is held to ~90 s of CPU work whatever --steps is:
-    # each step is a sample of (at least 128) rows sized to 90 s / steps
+    # each step is a sample of row blocks sized to 90 s / steps
     per_step = max(0.05, min(6.0, REFERENCE_ARM_SECONDS / max(1, args.steps)))
     t0 = time.perf_counter()
-    res = cpu_baseline(per_step, steps=args.steps)
+    res = cpu_baseline(args.n, per_step, steps=args.steps)
     wall = time.perf_counter() - t0
     pairs_step = res["value"] * res["seconds"] / args.steps
     line = {
@@ -146,7 +169,7 @@ def run_reference_arm(args) -> None:
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded 8-component Gaussian mixture)",
-        "config": workload_config(),
+        "config": workload_config(args.n),
         "cpu_baseline": {"value": res["value"], "unit": "pair-evals/s", "cores": res["cores"],
                          "kind": res["kind"], "sample": res["sample"]},
         "e2e": {"value": res["value"], "unit": "pair-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -154,6 +177,155 @@ def run_reference_arm(args) -> None:
                  f"warm-up {warm['seconds']:.1f}s, timed wall {wall:.1f}s",
     }
     print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# reference Triton leg (child process)
+# ---------------------------------------------------------------------------
+def triton_leg(n: int, h: float, steps: int, ieee: bool) -> dict:
+    """Runs this script with --triton-leg in a child process (the reference's
+    packages share module names with this package, so they get a process of
+    their own) and returns its JSON object."""
+    if not (REF_DIR / "kernels" / "flash_sd_kde").is_dir():
+        return {"unavailable": f"reference package not present under {REF_DIR.relative_to(ROOT)}"}
+    cmd = [sys.executable, str(ROOT / "bench.py"), "--triton-leg", "--n", str(n), "--h", repr(h),
+           "--triton-steps", str(steps)] + (["--triton-ieee"] if ieee else [])
+    env = dict(os.environ)
+    # Triton's bundled ptxas predates sm_103a; the toolkit's ptxas (CUDA 13)
+    # compiles the same PTX for this GPU.  TRITON_PTXAS_PATH is Triton's own
+    # switch for that; the reference's code is unchanged.
+    for cand in ("/usr/local/cuda/bin/ptxas",):
+        if os.path.exists(cand) and "TRITON_PTXAS_PATH" not in env:
+            env["TRITON_PTXAS_PATH"] = cand
+    try:
+        res = subprocess.run(cmd, cwd=str(ROOT), capture_output=True, text=True, timeout=1500, env=env)
+        out, err, rc = res.stdout, res.stderr, res.returncode
+    except subprocess.TimeoutExpired as exc:
+        out = exc.stdout.decode() if isinstance(exc.stdout, bytes) else (exc.stdout or "")
+        err, rc = "timed out after 1500 s", None
+    # the child prints its cumulative result after every leg
+    lines = [ln for ln in out.strip().splitlines() if ln.startswith("{")]
+    if not lines:
+        return {"unavailable": f"reference Triton leg failed (rc {rc}): {err.strip()[-600:]}"}
+    res = json.loads(lines[-1])
+    if rc != 0:
+        res["incomplete"] = f"rc {rc}: {err.strip()[-300:]}"
+    return res
+
+
+def run_triton_leg(args) -> None:
+    """Child process: the reference's own kernels, unmodified, from
+    baseline/_ref (its package directories as published), timed with CUDA
+    events on the same GMM8 workload.  Paper protocol
+    (experiments/runtime/benchmark_triton_kde.py:344-388 of the reference):
+    empirical_sd_kde_triton_nd + gaussian_kde_triton_nd; default public API:
+    emp_sd_kde_fit_transform + kde_eval (flash score backend, splitk_stream
+    KDE, fast_tf32, autotune)."""
+    import importlib.util
+
+    sys.path[:] = [str(REF_DIR)] + [p for p in sys.path if p not in (str(PKG), str(ROOT))] + [str(ROOT)]
+    import numpy as np
+    import torch
+
+    spec = importlib.util.spec_from_file_location("fsk_workloads", PKG / "fsk" / "workloads.py")
+    wl = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(wl)
+    import triton
+
+    import flash_sd_kde as ref_api
+    import kernels.flash_sd_kde as ref_k
+    for mod in (ref_api, ref_k):
+        if not str(Path(mod.__file__).resolve()).startswith(str(REF_DIR.resolve())):
+            raise RuntimeError(f"{mod.__name__} resolved outside {REF_DIR}")
+    from oracle import fp64
+
+    dev = torch.device("cuda", 0)
+    n, h = args.n, float(args.h)
+    gmm = wl.GMM16(seed=0)
+    x_np, q_np = gmm.sample(n, seed=1), gmm.sample(n, seed=2)
+    x = torch.from_numpy(x_np).to(dev)
+    q = torch.from_numpy(q_np).to(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def timed(fn, steps, warm):
+        for _ in range(warm):
+            out = fn()
+        torch.cuda.synchronize(dev)
+        ms = []
+        for _ in range(steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            out = fn()
+            e1.record()
+            torch.cuda.synchronize(dev)
+            ms.append(e0.elapsed_time(e1))
+        return ms, out
+
+    def paper_step():
+        deb, _ = ref_k.empirical_sd_kde_triton_nd(x, h, device=dev, return_tensor=True, synchronize=False)
+        return deb, ref_k.gaussian_kde_triton_nd(deb, q, h, device=dev, synchronize=False)
+
+    def api_step():
+        deb = ref_api.emp_sd_kde_fit_transform(x, h, device=dev)
+        return deb, ref_api.kde_eval(deb, q, h, device=dev)
+
+    pairs = 2.0 * n * n
+    out = {"impl": "reference-triton", "triton": triton.__version__, "torch": torch.__version__,
+           "ptxas": os.environ.get("TRITON_PTXAS_PATH", "triton bundled"),
+           "source": "baseline/_ref (the reference's flash_sd_kde/, kernels/, globals.py, unmodified)",
+           "workload": f"sdkde_gmm8_16d_n{n}_m{n}", "pairs_per_step": pairs, "bandwidth": h}
+    sub_q = 64
+    ref_logp = fp64.log_density(x_np, q_np[:sub_q], h)
+    # FP64 debias of rows 0..63 (self pair included)
+    rows = np.arange(64)
+    pdf64, w64 = fp64.empirical_score_rows(x_np, rows, h)
+    deb64 = x_np[:64].astype(np.float64) + 0.5 * (w64 / (pdf64[:, None] + EPS) - x_np[:64])
+
+    def errors(deb, kde_of_x):
+        dens = kde_of_x.detach().cpu().numpy().astype(np.float64)
+        rel = np.abs(dens - np.exp(ref_logp)) / np.exp(ref_logp)
+        return {"kde_max_rel_vs_fp64": float(rel.max()), "kde_median_rel_vs_fp64": float(np.median(rel)),
+                "kde_queries_checked": sub_q,
+                "debias_max_abs_vs_fp64": float(np.abs(deb[:64].detach().cpu().numpy() - deb64).max()),
+                "debias_rows_checked": 64}
+
+    legs = {}
+    out["legs"] = legs
+
+    def report():
+        best = max(legs, key=lambda k: legs[k]["pair_evals_per_s"])
+        out["best_leg"] = best
+        out["pair_evals_per_s"] = legs[best]["pair_evals_per_s"]
+        print(json.dumps(out), flush=True)
+
+    ms, (deb, _) = timed(paper_step, args.triton_steps, 1)
+    kde_x = ref_k.gaussian_kde_triton_nd(x, q[:sub_q], h, device=dev)
+    legs["paper_protocol_fast_tf32"] = {
+        "calls": "empirical_sd_kde_triton_nd + gaussian_kde_triton_nd",
+        "ms_per_step": statistics.median(ms), "step_ms": ms,
+        "pair_evals_per_s": pairs / (statistics.median(ms) * 1e-3), **errors(deb, kde_x)}
+    report()
+    ms, (deb, _) = timed(api_step, args.triton_steps, 2)
+    kde_x = ref_api.kde_eval(x, q[:sub_q], h, device=dev)
+    legs["default_api_fast_tf32"] = {
+        "calls": "emp_sd_kde_fit_transform + kde_eval (flash_sd_kde score backend, splitk_stream KDE, autotune)",
+        "ms_per_step": statistics.median(ms), "step_ms": ms,
+        "pair_evals_per_s": pairs / (statistics.median(ms) * 1e-3), **errors(deb, kde_x)}
+    report()
+    if args.triton_ieee:
+        def ieee_step():
+            deb = ref_api.emp_sd_kde_fit_transform(x, h, device=dev, precision_mode="fp32_ieee",
+                                                   emp_score_backend="symmetric_atomic")
+            return deb, ref_api.kde_eval(deb, q, h, device=dev, precision_mode="fp32_ieee")
+
+        ms, (deb, _) = timed(ieee_step, 1, 1)
+        kde_x = ref_api.kde_eval(x, q[:sub_q], h, device=dev, precision_mode="fp32_ieee")
+        legs["default_api_fp32_ieee"] = {
+            "calls": "emp_sd_kde_fit_transform(symmetric_atomic, fp32_ieee) + kde_eval(fp32_ieee)",
+            "ms_per_step": statistics.median(ms), "step_ms": ms,
+            "pair_evals_per_s": pairs / (statistics.median(ms) * 1e-3), **errors(deb, kde_x)}
+        report()
 
 
 # ---------------------------------------------------------------------------
@@ -223,18 +395,23 @@ def exp_peak(rates) -> dict:
 
 
 def tensor_roofline(kernel, pairs_per_s) -> dict | None:
-    """Tensor-pipe view of the dominant kernel: its fp16 MMA flops per second
-    against the measured dense bf16 peak (same tensor rate as fp16)."""
+    """Tensor-pipe view of the dominant kernel against the measured dense
+    bf16 peak (the fp16 tensor rate is the same): the algorithmic contraction
+    flops and the flops the kernel issues for its split-precision operands."""
     if not kernel or kernel not in MMA_FLOPS_PER_PAIR or not pairs_per_s:
         return None
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = peaks.get("bf16_tflops")
-    src = "MEASURED_PEAKS.json bf16_tflops (burst, cuBLAS)"
+    src = "MEASURED_PEAKS.json bf16_tflops (burst, cuBLAS), of measured"
     if not peak:
-        peak, src = 1900.0, "fallback 1.9 PFLOP/s"
-    achieved = pairs_per_s * MMA_FLOPS_PER_PAIR[kernel] / 1e12
-    return {"bound": "tensor", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak, "flops_per_pair": MMA_FLOPS_PER_PAIR[kernel], "peak_source": src}
+        peak, src = 1900.0, "fallback 1.9 PFLOP/s, of fallback"
+    fl = MMA_FLOPS_PER_PAIR[kernel]
+    alg = pairs_per_s * fl["algorithmic"] / 1e12
+    iss = pairs_per_s * fl["issued"] / 1e12
+    return {"bound": "tensor", "kernel": kernel, "achieved": alg, "peak": peak, "unit": "TFLOP/s",
+            "frac": alg / peak, "flops_per_pair": fl["algorithmic"],
+            "issued": {"achieved": iss, "frac": iss / peak, "flops_per_pair": fl["issued"]},
+            "peak_source": src}
 
 
 def run_gpu_arm(args) -> None:
@@ -253,31 +430,28 @@ def run_gpu_arm(args) -> None:
 
     ge.build()
     from flash_sd_kde import emp_sd_kde_fit_transform, kde_eval
-    from fsk import _lib, ops, workloads
+    from fsk import _lib, ops
     from oracle import fp64
 
     lib = _lib.load()
-    gmm = workloads.GMM16(seed=0)
-    x_np = gmm.sample(N_TRAIN, seed=1)
-    q_np = gmm.sample(N_QUERY, seed=2 + rank)
+    n = args.n
+    x_np, q_np = gmm_inputs(n, query_seed=2 + rank)
     x = torch.from_numpy(x_np).to(dev)
     q = torch.from_numpy(q_np).to(dev)
     h = float(ops.silverman(x).item())
-    norm = 1.0 / ((2.0 * math.pi) ** 8 * h ** 16 * N_TRAIN)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
 
-    def step():
-        pdf, w = ops.empscore16(x, h, variant="ordered")
-        deb = ops.debias16(x, pdf, w, h, EPS)
-        return deb, ops.kde16_sum(q, deb, h, out_scale=norm)
+    def step(xd, qd):
+        deb = emp_sd_kde_fit_transform(xd, h, device=dev)
+        return deb, kde_eval(deb, qd, h, device=dev)
 
     rates = np.zeros(3)
     _lib.check(lib.fsk_diag_pipe_rates(rates.ctypes.data, stream.cuda_stream), "pipe rates")
     peak = exp_peak(rates)
 
     for _ in range(args.warmup):
-        step()
+        step(x, q)
     ops.device_status(dev)
 
     # ---- device-resident timing -------------------------------------------------
@@ -292,7 +466,7 @@ def run_gpu_arm(args) -> None:
         for s_ev, e_ev in evs:
             flush.zero_()
             s_ev.record(stream)
-            deb, dens = step()
+            deb, dens = step(x, q)
             e_ev.record(stream)
         torch.cuda.synchronize(dev)
     lib.fsk_timer_enable(0)
@@ -310,36 +484,37 @@ def run_gpu_arm(args) -> None:
         total_ms = float(t.item())
         dist.barrier()
     ops.device_status(dev)
-    pairs_step = float(N_TRAIN) * N_TRAIN + float(N_TRAIN) * N_QUERY
+    pairs_step = 2.0 * float(n) * n
     value = world * pairs_step * args.steps / (total_ms * 1e-3)
 
     kernels = {}
     for r in range(max(rows, 0)):
         name = KERNEL_NAMES.get(int(ids[r]), str(int(ids[r])))
-        kernels[name] = {"launches": int(nl[r]), "ms": float(kms[r]), "pair_evals": float(kwork[r]),
-                         "pair_evals_per_s": float(kwork[r]) / (kms[r] * 1e-3) if kms[r] > 0 else None,
+        kernels[name] = {"launches": int(nl[r]), "ms": float(kms[r]), "exps": float(kwork[r]),
+                         "exps_per_s": float(kwork[r]) / (kms[r] * 1e-3) if kms[r] > 0 else None,
                          "share_of_step_time": float(kms[r]) / total_ms if total_ms > 0 else None}
     dom = max(kernels, key=lambda k: kernels[k]["ms"]) if kernels else None
-    achieved = kernels[dom]["pair_evals_per_s"] if dom else None
+    achieved = kernels[dom]["exps_per_s"] if dom else None
     traffic = None
     tfile = ROOT / "profiles" / "traffic.json"
     if dom and tfile.exists():
         try:
-            traffic = json.loads(tfile.read_text()).get(dom, {}).get("bytes_per_launch")
+            # per-launch DRAM bytes of the dominant kernel, from an ncu capture at this n
+            tr = json.loads(tfile.read_text()).get(dom, {}).get(str(n), {})
+            traffic = tr.get("bytes_per_launch")
         except ValueError:
             traffic = None
 
     # ---- end-to-end through the public API from host buffers ----------------------
     x_pin = torch.from_numpy(x_np).pin_memory()
     q_pin = torch.from_numpy(q_np).pin_memory()
-    out_pin = torch.empty(N_QUERY, dtype=torch.float32).pin_memory()
+    out_pin = torch.empty(n, dtype=torch.float32).pin_memory()
     e2e_evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
 
     def e2e_step():
         xd = x_pin.to(dev, non_blocking=True)
         qd = q_pin.to(dev, non_blocking=True)
-        debd = emp_sd_kde_fit_transform(xd, h, device=dev)
-        dd = kde_eval(debd, qd, h, device=dev)
+        _, dd = step(xd, qd)
         out_pin.copy_(dd, non_blocking=True)
 
     for _ in range(max(1, args.warmup)):
@@ -361,17 +536,22 @@ def run_gpu_arm(args) -> None:
     e2e_value = world * pairs_step * args.steps / (e2e_ms * 1e-3)
 
     # ---- accuracy spot check against FP64 ------------------------------------------
-    sub = slice(0, 128)
+    sub = slice(0, 64)
     deb_np = deb.cpu().numpy()
     dens_np = dens.cpu().numpy().astype(np.float64)
     ref_logp = fp64.log_density(deb_np, q_np[sub], h)
     kde_rel = np.abs(dens_np[sub] - np.exp(ref_logp)) / np.exp(ref_logp)
-    # debias of the first 64 rows against an FP64 score over the whole set
-    xs = x_np.astype(np.float64)
-    d2 = ((xs[:64, None, :] - xs[None, :, :]) ** 2).sum(-1)
-    phi = np.exp(-d2 / (2 * h * h))
-    deb64 = xs[:64] + 0.5 * ((phi @ xs) / (phi.sum(1, keepdims=True) + EPS) - xs[:64])
+    pdf64, w64 = fp64.empirical_score_rows(x_np, np.arange(64), h)
+    deb64 = x_np[:64].astype(np.float64) + 0.5 * (w64 / (pdf64[:, None] + EPS) - x_np[:64])
     deb_abs = float(np.abs(deb_np[:64] - deb64).max())
+
+    triton = None
+    if rank == 0 and not args.no_triton:
+        torch.cuda.synchronize(dev)
+        triton = triton_leg(n, h, args.triton_steps, args.triton_ieee)
+        if "pair_evals_per_s" in triton:
+            triton["value_vs_triton"] = value / triton["pair_evals_per_s"]
+            triton["e2e_vs_triton"] = e2e_value / triton["pair_evals_per_s"]
 
     surrogate = None
     if rank == 0 and not args.no_surrogate:
@@ -383,7 +563,7 @@ def run_gpu_arm(args) -> None:
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
-            cpu = cpu_baseline(12.0)
+            cpu = cpu_baseline(n, 12.0)
         except Exception as exc:  # reported, not fatal
             cpu = {"error": str(exc)[-300:]}
 
@@ -401,14 +581,14 @@ def run_gpu_arm(args) -> None:
             "vs_baseline": None,
             "dtype": "f32",
             "data": "synthetic (seeded 8-component Gaussian mixture)",
-            "config": workload_config(),
+            "config": workload_config(n),
             "e2e": {"value": e2e_value, "unit": "pair-evals/s",
-                    "h2d_bytes_per_step": int(x_np.nbytes + q_np.nbytes), "d2h_bytes_per_step": int(N_QUERY * 4),
+                    "h2d_bytes_per_step": int(x_np.nbytes + q_np.nbytes), "d2h_bytes_per_step": int(n * 4),
                     "ms_per_step": e2e_ms / args.steps,
                     "api": "flash_sd_kde.emp_sd_kde_fit_transform + flash_sd_kde.kde_eval"},
             "gpu_launches": int(launches),
             "roofline": {"bound": "sfu", "kernel": dom, "achieved": achieved, "peak": peak["peak"],
-                         "unit": "pair-evals/s (one exp per pair)",
+                         "unit": "required exps/s (one exp per pair; n(n+1)/2 for the symmetric score)",
                          "frac": (achieved / peak["peak"]) if achieved else None,
                          "traffic": traffic,
                          "peak_source": "measured on this GPU: ex2.approx %.3e/s, fma.f32 %.3e/s "
@@ -417,10 +597,11 @@ def run_gpu_arm(args) -> None:
                          "sfu_only_peak": peak["r_sfu"]},
             "roofline_tensor": tensor_roofline(dom, achieved),
             "kernels": kernels,
+            "triton_reference": triton,
             "cpu_baseline": cpu,
             "surrogate": surrogate,
             "clocks": sampler.summary(),
-            "accuracy": {"kde_max_rel_vs_fp64": float(kde_rel.max()), "kde_queries_checked": 128,
+            "accuracy": {"kde_max_rel_vs_fp64": float(kde_rel.max()), "kde_queries_checked": int(kde_rel.size),
                          "debias_max_abs_vs_fp64": deb_abs, "debias_rows_checked": 64},
             "step_ms": step_ms,
         }
@@ -480,14 +661,14 @@ def surrogate_workload(args, dev) -> dict:
     fin = torch.isfinite(exact)
     rel = (torch.exp((logp - exact).double()) - 1).abs()
     srv = served.bool() & fin
-    n = q.shape[0]
+    nq = q.shape[0]
     return {
-        "workload": f"surrogate_gmm8_16d_fit{args.sur_train}_pairs{args.sur_pairs}_eval{n}",
+        "workload": f"surrogate_gmm8_16d_fit{args.sur_train}_pairs{args.sur_pairs}_eval{nq}",
         "members": 4, "mlp": "16-256-256-256-1 SiLU, bf16 weights/activations, FP32 accumulation",
         "fit_seconds": fit_s, "train_mse_normalised": sur.history[-1] if sur.history else None,
-        "exact_queries_per_s": n / (ms_exact * 1e-3),
-        "gated_queries_per_s": n / (ms_gated * 1e-3),
-        "surrogate_only_queries_per_s": n / (ms_sur * 1e-3),
+        "exact_queries_per_s": nq / (ms_exact * 1e-3),
+        "gated_queries_per_s": nq / (ms_gated * 1e-3),
+        "surrogate_only_queries_per_s": nq / (ms_sur * 1e-3),
         "speedup_gated_vs_exact": ms_exact / ms_gated,
         "speedup_surrogate_only_vs_exact": ms_exact / ms_sur,
         "served_fraction": float(srv.float().mean()),
@@ -514,6 +695,58 @@ def run_surrogate(args) -> None:
     print(json.dumps({"surrogate": surrogate_workload(args, dev)}), flush=True)
 
 
+def run_precision(args) -> None:
+    """The precision-stress configuration: n_train = n_query (default 2^20)
+    multivariate Student-t (nu = 5) points, per-axis scale 10^U(-1, 1), +100
+    offset; h in {0.5, 1, 2} x Silverman of the training set; every distance
+    mode of the 16-D KDE (three-part fp16 tensor-core products with the exact
+    near-pair recompute; FP32 direct differences; the single-pass fp16 rung;
+    the exact-log output) over all queries, with FP64 log-density errors on a
+    fixed 4096-query subset (max / mean / p95 absolute log error, as the
+    reference's error suite reports them) and each mode's time."""
+    import numpy as np
+    import torch
+
+    import __graft_entry__ as ge
+
+    ge.build()
+    from fsk import ops, workloads
+    from oracle import fp64
+
+    dev = torch.device("cuda", 0)
+    n = args.n
+    x_np = workloads.student_t_16d(n, seed=4)
+    q_np = workloads.student_t_16d(n, seed=5)
+    x = torch.from_numpy(x_np).to(dev)
+    q = torch.from_numpy(q_np).to(dev)
+    h0 = float(ops.silverman(x).item())
+    sub = np.random.default_rng(0).choice(n, min(n, 4096), replace=False)
+    rows = []
+    for f in (0.5, 1.0, 2.0):
+        h = h0 * f
+        norm = 1.0 / ((2 * math.pi) ** 8 * h ** 16 * n)
+        ref = fp64.log_density_gemm(x_np, q_np[sub], h)
+        for mode in ("tensor", "ieee", "fp16_single", "tensor_log_exact"):
+            if mode == "tensor_log_exact":
+                fn = lambda: ops.kde16_sum(q, x, h, out_scale=norm, log_exact=True)
+            else:
+                fn = lambda mode=mode: ops.kde16_sum(q, x, h, precision=mode, out_scale=norm, log_eps=0.0)
+            fn()
+            torch.cuda.synchronize(dev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            lp = fn()
+            e1.record()
+            torch.cuda.synchronize(dev)
+            ops.device_status(dev)
+            got = lp.cpu().numpy().astype(np.float64)[sub]
+            rows.append({"h_factor": f, "h": h, "mode": mode, "ms": e0.elapsed_time(e1),
+                         **fp64.log_error_metrics(got, ref)})
+            print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
+    print(json.dumps({"op": "precision", "workload": f"student_t5_offset100_16d_n{n}_m{n}",
+                      "queries_checked": int(sub.size), "silverman_h": h0, "rows": rows}), flush=True)
+
+
 def run_op(args) -> None:
     """One operation alone (the profiling case for ncu captures): n GMM8
     points as data and as queries, Silverman bandwidth, W warm-up and K timed
@@ -527,6 +760,8 @@ def run_op(args) -> None:
 
     import __graft_entry__ as ge
 
+    if args.op == "precision":
+        return run_precision(args)
     ge.build()
     from fsk import ops, workloads
 
@@ -544,15 +779,19 @@ def run_op(args) -> None:
         return _time_op(args, dev, fn, pairs, h1)
     x = torch.from_numpy(workloads.GMM16(seed=0).sample(args.n, seed=1)).to(dev)
     h = float(ops.silverman(x).item())
+    pairs = float(args.n) * args.n
     if args.op == "kde16":
         fn = lambda: ops.kde16_sum(x, x, h)
     elif args.op == "kde16_logexact":
         q = x.clone()
         q[::2] += 60.0 * h / 4.0      # offset 15 h per feature: 60 h away in 16-D
         fn = lambda: ops.kde16_sum(q, x, h, log_exact=True)
+    elif args.op == "score16_sym":
+        fn = lambda: ops.empscore16(x, h, variant="symmetric")
+        pairs = float(args.n) * (args.n + 1) / 2.0
     else:
         fn = lambda: ops.empscore16(x, h)
-    _time_op(args, dev, fn, float(args.n) * args.n, h)
+    _time_op(args, dev, fn, pairs, h)
 
 
 def fp_sdkde_1d(x) -> float:
@@ -582,11 +821,14 @@ def _time_op(args, dev, fn, pairs, h) -> None:
     ops.device_status(dev)
     ms = s_ev.elapsed_time(e_ev) / args.steps
     print(json.dumps({"op": args.op, "n": args.n, "h": h, "ms_per_call": ms,
-                      "pair_evals_per_s": pairs / (ms * 1e-3)}), flush=True)
+                      "required_exps_per_s": pairs / (ms * 1e-3)}), flush=True)
 
 
 def main():
     args = parse()
+    if args.triton_leg:
+        run_triton_leg(args)
+        return
     if args.op:
         run_op(args)
         return

@@ -81,8 +81,8 @@ size_t kde16_bytes(int64_t m, int64_t n, const Kde16Plan& p) {
   return align_up(c.used, 256);
 }
 
-constexpr int KNOWN_FLAGS =
-    FSK_PREC_IEEE | FSK_LAPLACE | FSK_OUT_LOG | FSK_ATOMIC | FSK_WEIGHTED_FEATURE_MAJOR | FSK_OUT_LOG_EXACT;
+constexpr int KNOWN_FLAGS = FSK_PREC_IEEE | FSK_LAPLACE | FSK_OUT_LOG | FSK_ATOMIC | FSK_WEIGHTED_FEATURE_MAJOR |
+                            FSK_OUT_LOG_EXACT | FSK_PREC_FP16_SINGLE;
 
 // FSK_OUT_LOG_EXACT: only with FSK_OUT_LOG, out_eps = 0 and m < 2^32 (list indices)
 bool bad_log_exact(int flags, double out_eps, int64_t m) {
@@ -91,6 +91,16 @@ bool bad_log_exact(int flags, double out_eps, int64_t m) {
 }
 
 }  // namespace
+
+int validate_kde16_args(const float* q, int64_t m, const float* x, int64_t n, double h, int flags,
+                        double out_eps, const float* out) {
+  if (!q || !x || !out || m < 1 || n < 1 || bad_bw(h)) return FSK_ERR_INVALID_ARGUMENT;
+  if (flags & ~KNOWN_FLAGS) return FSK_ERR_INVALID_ARGUMENT;
+  if ((flags & FSK_PREC_FP16_SINGLE) && (flags & FSK_PREC_IEEE)) return FSK_ERR_INVALID_ARGUMENT;
+  if (bad_log_exact(flags, out_eps, m)) return FSK_ERR_INVALID_ARGUMENT;
+  return FSK_OK;
+}
+
 }  // namespace fsk
 
 using namespace fsk;
@@ -136,10 +146,9 @@ size_t fsk_kde16_workspace_bytes(int64_t m, int64_t n, int flags) {
 int fsk_kde16(const float* queries, int64_t m, const float* data, int64_t n, double bandwidth, int flags,
               double out_scale, double out_eps, float* out, void* workspace, size_t workspace_bytes,
               void* stream) {
-  if (!queries || !data || !out || m < 1 || n < 1 || bad_bw(bandwidth)) return FSK_ERR_INVALID_ARGUMENT;
-  if (flags & ~KNOWN_FLAGS) return FSK_ERR_INVALID_ARGUMENT;
-  if (bad_log_exact(flags, out_eps, m)) return FSK_ERR_INVALID_ARGUMENT;
-  int st = check_device();
+  int st = validate_kde16_args(queries, m, data, n, bandwidth, flags, out_eps, out);
+  if (st) return st;
+  st = check_device();
   if (st) return st;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const Kde16Plan p = plan16(m, n, flags);
@@ -158,7 +167,8 @@ int fsk_kde16(const float* queries, int64_t m, const float* data, int64_t n, dou
                       p.atomic ? nullptr : part, p.atomic ? part : nullptr, s);
   } else {
     launch_mean16(data, n, cb.scratch, cb.mu, cb.mu64, s);
-    st = tc::launch_kde16_tc(queries, m, data, n, cb.mu, bandwidth, laplace, p.tcp, c, &part, p.atomic, s);
+    st = tc::launch_kde16_tc(queries, m, data, n, cb.mu, bandwidth, laplace, (flags & FSK_PREC_FP16_SINGLE) != 0,
+                             p.tcp, c, &part, p.atomic, s);
     if (st) return st;
     splits = p.atomic ? 1 : (int)p.tcp.part_rows;
   }
@@ -174,21 +184,21 @@ int fsk_kde16(const float* queries, int64_t m, const float* data, int64_t n, dou
 }
 
 // ---- empirical score ------------------------------------------------------------
-// Tensor precision: the tcgen05 ordered kernel for both variants (the
-// symmetric variant is the same quantity; on GB300 the tensor-core product
-// is cheaper than halving the exps on CUDA cores).  FSK_PREC_IEEE: the
-// CUDA-core kernels of the requested variant.
+// Ordered variant: the tcgen05 split-K kernel (tensor precision) or the
+// CUDA-core split-K kernel (FSK_PREC_IEEE).  Symmetric variant: the
+// upper-triangle kernel, each pair's exp evaluated once, row and column sums
+// scattered with FP64 atomics.
 static size_t empscore_bytes(int64_t n, int variant, int flags) {
   WsCarver c(nullptr, 0);
   take_center(c, n);
   c.take<double>(reduce_score_scratch_doubles(n));
   size_t b = c.used;
-  if (!(flags & FSK_PREC_IEEE)) {
-    b = align_up(b, 256) + tc::tc_score16_ws_bytes(tc::plan_score16(n), n);
-  } else if (variant == FSK_SCORE_SYMMETRIC) {
+  if (variant == FSK_SCORE_SYMMETRIC) {
     c.take<double>((size_t)n);
     c.take<double>((size_t)n * FSK_D);
     b = c.used;
+  } else if (!(flags & FSK_PREC_IEEE)) {
+    b = align_up(b, 256) + tc::tc_score16_ws_bytes(tc::plan_score16(n), n);
   } else {
     const int splits = simt_score16_splits(n);
     c.take<double>((size_t)splits * n);
@@ -207,7 +217,7 @@ int fsk_empscore16(const float* data, int64_t n, double bandwidth, int variant, 
                    float* weighted_sum, void* workspace, size_t workspace_bytes, void* stream) {
   if (!data || !pdf_sum || !weighted_sum || n < 1 || bad_bw(bandwidth)) return FSK_ERR_INVALID_ARGUMENT;
   if (variant != FSK_SCORE_ORDERED && variant != FSK_SCORE_SYMMETRIC) return FSK_ERR_INVALID_ARGUMENT;
-  if (flags & ~KNOWN_FLAGS) return FSK_ERR_INVALID_ARGUMENT;
+  if (flags & ~(KNOWN_FLAGS & ~FSK_PREC_FP16_SINGLE)) return FSK_ERR_INVALID_ARGUMENT;
   int st = check_device();
   if (st) return st;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -218,20 +228,20 @@ int fsk_empscore16(const float* data, int64_t n, double bandwidth, int variant, 
   launch_mean16(data, n, cb.scratch, cb.mu, cb.mu64, s);
   const bool fm = (flags & FSK_WEIGHTED_FEATURE_MAJOR) != 0;
   const int64_t ws_row = fm ? 1 : FSK_D, ws_col = fm ? n : 1;
-  if (!(flags & FSK_PREC_IEEE)) {
-    const tc::TcPlan pl = tc::plan_score16(n);
-    double *ppdf = nullptr, *pw = nullptr;
-    st = tc::launch_score16_tc(data, n, cb.mu, bandwidth, pl, c, &ppdf, &pw, s);
-    if (st) return st;
-    launch_reduce_score(ppdf, pw, (int)(2 * pl.splits), (int)pl.splits, n, cb.mu64, data, pdf_sum,
-                        weighted_sum, ws_row, ws_col, rscratch, s);
-  } else if (variant == FSK_SCORE_SYMMETRIC) {
+  if (variant == FSK_SCORE_SYMMETRIC) {
     double* apdf = c.take<double>((size_t)n);
     double* aw = c.take<double>((size_t)n * FSK_D);
     launch_zero(apdf, n, s);
     launch_zero(aw, n * FSK_D, s);
     launch_score16_sym_simt(data, n, cb.mu, bandwidth, apdf, aw, s);
     launch_reduce_score(apdf, aw, 1, 1, n, cb.mu64, nullptr, pdf_sum, weighted_sum, ws_row, ws_col, rscratch, s);
+  } else if (!(flags & FSK_PREC_IEEE)) {
+    const tc::TcPlan pl = tc::plan_score16(n);
+    double *ppdf = nullptr, *pw = nullptr;
+    st = tc::launch_score16_tc(data, n, cb.mu, bandwidth, pl, c, &ppdf, &pw, s);
+    if (st) return st;
+    launch_reduce_score(ppdf, pw, (int)(2 * pl.splits), (int)pl.splits, n, cb.mu64, data, pdf_sum,
+                        weighted_sum, ws_row, ws_col, rscratch, s);
   } else {
     const int splits = simt_score16_splits(n);
     double* ppdf = c.take<double>((size_t)splits * n);

@@ -95,6 +95,34 @@ __device__ __forceinline__ float ex2_approx(float x) {
   return y;
 }
 
+// 2^a for a <= 0 on the FP32 FMA pipe, two lanes per instruction: the
+// exp pipe's work moved to the FMA pipe where that pipe has spare issue
+// slots.  a = j + r with j = round(a) (adding 1.5 * 2^23 leaves j in the low
+// mantissa bits) and r in [-1/2, 1/2]; 2^r from a degree-5 polynomial whose
+// coefficients minimise the maximum relative error on [-1/2, 1/2] (Remez
+// exchange, csrc/exp2_poly_remez.py; 7.5e-8 in exact arithmetic, 2.1e-7 with
+// the FP32 Horner evaluation, about the error of ex2.approx.f32); j is added
+// to the exponent field by one integer multiply-add.  Inputs below -125 are
+// clamped (result ~2^-125 * 2^r, where ex2.approx.ftz returns 0 for
+// a < -126: negligible against any sum with a term above 2^-100).
+__device__ __forceinline__ float2 exp2_poly2(float2 a) {
+  const float2 magic = make_float2(12582912.0f, 12582912.0f);   // 1.5 * 2^23
+  a.x = fmaxf(a.x, -125.0f);
+  a.y = fmaxf(a.y, -125.0f);
+  const float2 t = __fadd2_rn(a, magic);
+  const float2 j = __fadd2_rn(t, make_float2(-12582912.0f, -12582912.0f));      // round(a), exact
+  const float2 r = __ffma2_rn(j, make_float2(-1.0f, -1.0f), a);                 // a - j, exact
+  float2 p = __ffma2_rn(make_float2(1.327647245e-03f, 1.327647245e-03f), r,
+                        make_float2(9.675540961e-03f, 9.675540961e-03f));
+  p = __ffma2_rn(p, r, make_float2(5.550713092e-02f, 5.550713092e-02f));
+  p = __ffma2_rn(p, r, make_float2(2.402212024e-01f, 2.402212024e-01f));
+  p = __ffma2_rn(p, r, make_float2(6.931469440e-01f, 6.931469440e-01f));
+  p = __ffma2_rn(p, r, make_float2(1.000000119e+00f, 1.000000119e+00f));
+  // (bits(t) << 23) == (j << 23) mod 2^32: the magic's low nine bits are zero
+  return make_float2(__uint_as_float((__float_as_uint(t.x) << 23) + __float_as_uint(p.x)),
+                     __uint_as_float((__float_as_uint(t.y) << 23) + __float_as_uint(p.y)));
+}
+
 // Packed two-lane FP32 add / fma (one issue slot for two lane operations).
 __device__ __forceinline__ void fadd2(float& d0, float& d1, float a0, float a1, float b0, float b1) {
   uint64_t ra, rb, rd;

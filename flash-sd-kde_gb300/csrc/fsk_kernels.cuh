@@ -4,6 +4,12 @@
 
 namespace fsk {
 
+// ---- fsk_api.cu -------------------------------------------------------------
+// Argument checks of fsk_kde16 (pointers, sizes, bandwidth, flags and the
+// FSK_OUT_LOG_EXACT constraints): FSK_OK or FSK_ERR_INVALID_ARGUMENT.
+int validate_kde16_args(const float* q, int64_t m, const float* x, int64_t n, double h, int flags,
+                        double out_eps, const float* out);
+
 // ---- fsk_simt.cu ------------------------------------------------------------
 void launch_kde16_simt(const float* q, int64_t m, const float* x, int64_t n, double h, bool laplace,
                        int splits, double* partials, double* atomic_acc, cudaStream_t s);

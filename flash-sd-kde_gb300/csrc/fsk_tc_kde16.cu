@@ -54,7 +54,10 @@
 namespace fsk {
 namespace tc {
 
-template <bool LAPLACE>
+// SINGLE: the single-pass precision rung (FSK_PREC_FP16_SINGLE) - only the
+// hi.hi cross product (one fp16 product per feature, FP32 accumulation) and
+// the bias step, no exact near-pair recompute.
+template <bool LAPLACE, bool SINGLE>
 __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* sA = smem_raw;                               // NQT query tiles: H | M | L
@@ -173,7 +176,10 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
           tc_fence_after();
           const uint64_t so = (uint64_t)(s * (KB_STAGE_BYTES >> 4));
           if (lane == 0) {
-            mma_s_tile(d0 + b * (uint32_t)(NQT * KNT), a_h, a_m, a_l, b_h0 + so, b_m0 + so, b_l0 + so, idesc);
+            if (SINGLE)
+              mma_s_tile_single(d0 + b * (uint32_t)(NQT * KNT), a_h, b_h0 + so, idesc);
+            else
+              mma_s_tile(d0 + b * (uint32_t)(NQT * KNT), a_h, a_m, a_l, b_h0 + so, b_m0 + so, b_l0 + so, idesc);
             mma_commit(&tfull[b * NQT + a]);
             mma_commit(&empty[s]);
           }
@@ -285,8 +291,8 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
             // Near-pair test: a chunk holding more than NEAR_FRACTION of the
             // running sum (this chunk included) may contain a dominant term.
             const float run = s_carry + fabsf(acc.s) + fabsf(tsum);
-            const bool trig = fabsf(cs) > (run + fabsf(cs)) * NEAR_FRACTION;
-            if (__any_sync(0xffffffffu, trig)) {
+            const bool trig = !SINGLE && fabsf(cs) > (run + fabsf(cs)) * NEAR_FRACTION;
+            if (!SINGLE && __any_sync(0xffffffffu, trig)) {
               // Triggered lanes replace their chunk's largest term by its exact
               // value.  The argmax rides in the low 5 mantissa bits of each term
               // (key = |e| with bits[4:0] := column); the chunk is re-summed
@@ -544,8 +550,17 @@ size_t tc_kde16_ws_bytes(const TcPlan& pl, int64_t m, bool atomic) {
   return b;
 }
 
+template <bool LAPLACE, bool SINGLE>
+static cudaError_t launch_kde16_tc_kernel(const TcPlan& pl, const TcParams& p, cudaStream_t s) {
+  const cudaError_t e = cudaFuncSetAttribute(kde16_tc_kernel<LAPLACE, SINGLE>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+  if (e != cudaSuccess) return e;
+  kde16_tc_kernel<LAPLACE, SINGLE><<<pl.grid, THREADS, SMEM_BYTES, s>>>(p);
+  return cudaGetLastError();
+}
+
 int launch_kde16_tc(const float* q, int64_t m, const float* x, int64_t n, const float* mu, double h,
-                    bool laplace, const TcPlan& pl, WsCarver& c, double** partials_out, bool atomic,
+                    bool laplace, bool single, const TcPlan& pl, WsCarver& c, double** partials_out, bool atomic,
                     cudaStream_t s) {
   TcScales* sc = c.take<TcScales>(1);
   uint8_t* qimg = c.take<uint8_t>((size_t)pl.q_blocks * A_BYTES);
@@ -593,17 +608,12 @@ int launch_kde16_tc(const float* q, int64_t m, const float* x, int64_t n, const 
   p.atomic_acc = atomic ? part : nullptr;
   cudaError_t e;
   TimerScope ts(K_KDE16_TC, (double)m * (double)n, s);
-  if (laplace) {
-    e = cudaFuncSetAttribute(kde16_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-    if (e != cudaSuccess) return cuda_status(e);
-    kde16_tc_kernel<true><<<pl.grid, THREADS, SMEM_BYTES, s>>>(p);
-  } else {
-    e = cudaFuncSetAttribute(kde16_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-    if (e != cudaSuccess) return cuda_status(e);
-    kde16_tc_kernel<false><<<pl.grid, THREADS, SMEM_BYTES, s>>>(p);
-  }
+  if (laplace)
+    e = single ? launch_kde16_tc_kernel<true, true>(pl, p, s) : launch_kde16_tc_kernel<true, false>(pl, p, s);
+  else
+    e = single ? launch_kde16_tc_kernel<false, true>(pl, p, s) : launch_kde16_tc_kernel<false, false>(pl, p, s);
   count_launch();
-  return cuda_status(cudaGetLastError());
+  return cuda_status(e);
 }
 
 // ---- layout probe: D (128 x 64) = A (128 x 32) . B (64 x 32)^T, fp16 ----------------

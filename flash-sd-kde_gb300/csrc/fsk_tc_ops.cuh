@@ -39,6 +39,14 @@ __device__ __forceinline__ void mma_s_tile(uint32_t d, uint64_t a_h, uint64_t a_
   mma_f16_ss(d, a_h + bias, b_h + bias, idesc, 1u);   // beta_j + alpha_i
 }
 
+// Single-pass rung: hi.hi cross product and the bias K step (two MMAs); the
+// norms in the bias columns keep their three-part precision.
+__device__ __forceinline__ void mma_s_tile_single(uint32_t d, uint64_t a_h, uint64_t b_h, uint32_t idesc) {
+  const uint64_t bias = 256 >> 4;
+  mma_f16_ss(d, a_h, b_h, idesc, 0u);
+  mma_f16_ss(d, a_h + bias, b_h + bias, idesc, 1u);
+}
+
 // sum_k (q_k - x_k)^2 from the original FP32 coordinates of data row r.
 __device__ __forceinline__ float exact_dist(const uint8_t* stage, int r, const float (&q)[FSK_D],
                                             int x_offset = B_X_OFFSET) {

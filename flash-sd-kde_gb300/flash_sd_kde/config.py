@@ -2,9 +2,13 @@
 flash_sd_kde/config.py of the reference, same names and error messages).
 
 Tile shapes of the GB300 kernels are fixed by the hardware mapping (one query
-row per TMEM lane, 128-wide data tiles), so the reference's Triton tuning
-dataclasses are kept for API compatibility only.  ``cap_splits_for_memory``
-is implemented as in the reference (config.py:90-103).
+row per TMEM lane, 128-wide data tiles) and their split counts are chosen by
+the C planner (plan_splits in csrc/fsk_tc_kde16.cu, which bounds the FP64
+partial buffers), so the Triton tuning names below -- SplitKParams,
+SymmetricParams, compute_splitk_splits, cap_splits_for_memory,
+iter_autotune_candidates -- are kept only so code written against the
+reference's module still imports and computes the same numbers; nothing in
+this package's kernel path calls them.
 """
 from __future__ import annotations
 
@@ -86,6 +90,9 @@ def select_emp_score_backend(n: int, *, heuristics: KernelHeuristics = DEFAULT_H
 
 
 def compute_splitk_splits(n_data: int, *, block_n_iter: int, iters_per_split: int) -> int:
+    """Compatibility name: split count of the reference's Triton split-K grid
+    (ceil(n_data / (block_n_iter * iters_per_split))); not used by the GB300
+    kernels."""
     total = block_n_iter * iters_per_split
     if total <= 0:
         raise ValueError("block_n_total must be positive.")
@@ -99,6 +106,9 @@ def cap_splits_for_memory(
     features: int,
     heuristics: KernelHeuristics = DEFAULT_HEURISTICS,
 ) -> int:
+    """Compatibility name: the largest split count whose FP32 weighted
+    partials (n_query x features per split) fit the heuristic byte budget.
+    The GB300 path bounds its own FP64 partial buffers in the C planner."""
     if n_splits <= 1:
         return n_splits
     bytes_per_split = n_query * features * 4
@@ -109,4 +119,6 @@ def cap_splits_for_memory(
 
 
 def iter_autotune_candidates(candidates: Iterable[SplitKParams]) -> list[SplitKParams]:
+    """Compatibility name: the Triton autotune candidates as a list (the GB300
+    kernels have fixed tile shapes and no autotuning)."""
     return list(candidates)

@@ -102,6 +102,10 @@ def kde16_sum(
 ) -> torch.Tensor:
     """out[i] = out_scale * sum_j phi(q_i, x_j)  (or log(out_scale*sum + log_eps)).
 
+    precision "tensor" (three-part fp16 tensor-core products + exact near-pair
+    recompute), "ieee" (FP32 direct differences, CUDA cores) or "fp16_single"
+    (one fp16 cross product, no recompute: the lowest precision rung).
+
     log_exact: out[i] = log(out_scale * sum) without the eps floor and without
     underflow (queries whose sum underflows are recomputed with a
     running-minimum shift); needs log_eps None or 0.
@@ -113,7 +117,9 @@ def kde16_sum(
     m, n = q.shape[0], x.shape[0]
     if m == 0 or n == 0:
         raise ValueError("data and queries must contain at least one sample.")
-    flags = (L.FSK_PREC_IEEE if precision == "ieee" else L.FSK_PREC_TENSOR)
+    if precision not in ("tensor", "ieee", "fp16_single"):
+        raise ValueError(f"unknown precision {precision!r}")
+    flags = {"tensor": L.FSK_PREC_TENSOR, "ieee": L.FSK_PREC_IEEE, "fp16_single": L.FSK_PREC_FP16_SINGLE}[precision]
     flags |= (L.FSK_LAPLACE if laplace else 0) | (L.FSK_ATOMIC if atomic else 0)
     if log_exact:
         if log_eps:

@@ -14,7 +14,7 @@
  *
  * Reference interfaces replaced (paths inside the Flash-SD-KDE project):
  *   fsk_kde16        kernels/kde_eval_16d_stream_splitk.py:263 (kde_eval_16d_splitk),
- *                    :373 (kde_eval_16d_atomic), kernels/flash_sd_kde/kde.py:374
+ *                    :373 (kde_eval_16d_atomic), kernels/flash_sd_kde/kde.py:242
  *                    (gaussian_kde_triton_nd) and the normalisation in
  *                    flash_sd_kde/kde.py:119-122
  *   fsk_empscore16   kernels/flash_sd_kde/empirical.py:134 (emp_score_16d_flash_sd_kde),
@@ -69,6 +69,11 @@ enum fsk_status {
 /* precision_mode "fp32_ieee": every pair by FP32 direct differences on the
  * CUDA cores, no tensor cores. */
 #define FSK_PREC_IEEE 0x1
+/* fsk_kde16 only, no counterpart in the reference: the lowest rung of the
+ * precision ladder - the cross product as one fp16 product per feature
+ * (FP32 accumulation; the norms keep their three-part precision), no exact
+ * near-pair recompute.  For precision studies; not an exact mode. */
+#define FSK_PREC_FP16_SINGLE 0x40
 /* Laplace-corrected ("linearized") kernel phi * (1 + d/2 - dist/(2 h^2)),
  * kernels/kde_eval_16d_stream_splitk.py:75-76. */
 #define FSK_LAPLACE 0x2
@@ -117,8 +122,12 @@ FSK_API int fsk_kde16(const float* queries, int64_t m, const float* data, int64_
  * by every GPU that loads the library.  Requests needing more
  * (fsk_kde16_workspace_bytes) fail with FSK_ERR_SCRATCH_LIMIT.  All calls
  * share the array: calls whose GPU work overlaps race and must be
- * serialised.  The first call on a device looks up the array's address;
- * make it before any stream capture.  Allocates nothing. */
+ * serialised.  Argument errors are reported as by fsk_kde16
+ * (FSK_ERR_INVALID_ARGUMENT) before the size check.  Every call looks up
+ * the array's address in the current CUDA context (so context switches and
+ * cudaDeviceReset are safe); the first call in a context loads the
+ * library's device code, so make it before any stream capture in that
+ * context.  Allocates nothing. */
 #define FSK_NOALLOC_SCRATCH_BYTES (32u << 20)
 FSK_API int fsk_kde16_noalloc(const float* queries, int64_t m, const float* data, int64_t n,
                               double bandwidth, int flags, double out_scale, double out_eps,

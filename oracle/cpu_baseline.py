@@ -28,7 +28,11 @@ sys.path[:0] = [str(ROOT / "flash-sd-kde_gb300"), str(ROOT)]
 
 from oracle import reference_numpy as R  # noqa: E402
 
-BLOCK = 128
+BLOCK = 128          # rows per work item at n <= 65536; fewer above (memory per item ~ rows * n * 12 B)
+
+
+def block_rows(n: int) -> int:
+    return max(8, min(BLOCK, BLOCK * 65536 // max(1, n)))
 
 
 def _score_block(x, rows, h):
@@ -49,11 +53,12 @@ def run(x, q, h, rows: int, threads: int) -> tuple[float, float]:
     """Time the score of `rows` data rows plus the KDE of `rows` queries;
     returns (seconds, pair evaluations)."""
     n = x.shape[0]
-    starts = list(range(0, rows, BLOCK))
+    blk = block_rows(n)
+    starts = list(range(0, rows, blk))
     t0 = time.perf_counter()
     with cf.ThreadPoolExecutor(max_workers=threads) as ex:
-        futs = [ex.submit(_score_block, x, slice(s, min(rows, s + BLOCK)), h) for s in starts]
-        futs += [ex.submit(_kde_block, x, q[s:min(rows, s + BLOCK)], h) for s in starts]
+        futs = [ex.submit(_score_block, x, slice(s, min(rows, s + blk)), h) for s in starts]
+        futs += [ex.submit(_kde_block, x, q[s:min(rows, s + blk)], h) for s in starts]
         for f in futs:
             f.result()
     dt = time.perf_counter() - t0
@@ -72,10 +77,11 @@ def main() -> None:
     x, q = workloads.gmm8_16d(args.n, args.n)
     h = R.silverman_bandwidth_nd(x)
     # calibrate on one block per thread, then size the sample to the target
-    dt, pairs = run(x, q, h, BLOCK * args.threads, args.threads)
+    blk = block_rows(args.n)
+    dt, pairs = run(x, q, h, blk * args.threads, args.threads)
     rate = pairs / dt
-    rows = int(min(args.n, max(BLOCK, args.target_seconds * rate / (2.0 * args.n))))
-    rows = max(BLOCK, rows // BLOCK * BLOCK)
+    rows = int(min(args.n, max(blk, args.target_seconds * rate / (2.0 * args.n))))
+    rows = max(blk, rows // blk * blk)
     times = []
     for _ in range(args.steps):
         dt, pairs = run(x, q, h, rows, args.threads)

@@ -1,7 +1,8 @@
 """Generate tests/golden/*.npz by running the reference project's own CPU code.
 
-Run (where the reference checkout is available, e.g. at /root/reference):
-    python tests/golden/make_golden.py /root/reference
+Run where a checkout of the reference project is available, passing its root
+directory (required):
+    python tests/golden/make_golden.py <reference-checkout>
 
 It imports the reference's flash_sd_kde.reference (FP32 numpy path) and its
 FP64 log-space oracle (experiments/error_suite_16d/reference.py, with a stub
@@ -109,4 +110,6 @@ def main(root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <reference-checkout>")
+    main(sys.argv[1])

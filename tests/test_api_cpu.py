@@ -141,3 +141,32 @@ def test_shard_partition_covers_rows():
             spans = [shard(count, world, r) for r in range(world)]
             assert spans[0][0] == 0 and spans[-1][1] == count
             assert all(spans[i][1] == spans[i + 1][0] for i in range(world - 1))
+
+
+def test_exp2_poly_coefficients_and_error_bound():
+    """The FMA-pipe exp2 (fsk_common.cuh, exp2_poly2) uses the coefficients
+    its Remez generator (csrc/exp2_poly_remez.py) produces, and its FP32
+    evaluation (round to nearest, exponent-field insertion) stays within
+    2.5e-7 relative of FP64 2^x over x in [-125, 0] -- the error class of
+    ex2.approx.f32."""
+    import importlib.util
+    import re
+
+    import numpy as np
+
+    from conftest import PKG
+
+    src = (PKG / "csrc" / "fsk_common.cuh").read_text()
+    body = src[src.index("float2 exp2_poly2"):]
+    body = body[:body.index("\n}\n")]
+    consts = [float(v) for v in re.findall(r"make_float2\(([0-9.e+-]+)f, \1f\)", body)]
+    coeffs = [c for c in consts if 0.0 < c < 2.0]         # the polynomial (not the magic or the -1)
+    spec = importlib.util.spec_from_file_location("remez", PKG / "csrc" / "exp2_poly_remez.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    c, err = mod.remez()
+    want = [float(np.float32(v)) for v in c[::-1]]       # Horner order: c5 first
+    assert len(coeffs) == 6
+    np.testing.assert_allclose(coeffs, want, rtol=1e-8)
+    assert err < 1e-7
+    assert mod.fp32_check(c) < 2.5e-7

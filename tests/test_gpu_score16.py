@@ -72,17 +72,63 @@ def test_score_vs_reference(cuda_dev, golden, seed, variant):
     _close(w.cpu().numpy(), w64, rtol=2e-6, floor=2e-6)
 
 
-def test_symmetric_matches_ordered_1024(cuda_dev, golden):
+def _kernel_ids(fn):
+    """Library kernel ids (fsk.h measurement hooks) launched by fn()."""
+    from fsk import _lib as L
+
+    lib = L.load()
+    torch.cuda.synchronize()
+    ids, nl = np.zeros(16, np.int32), np.zeros(16, np.int64)
+    ms, work = np.zeros(16), np.zeros(16)
+    lib.fsk_timer_collect(ids.ctypes.data, nl.ctypes.data, ms.ctypes.data, work.ctypes.data, 16)
+    lib.fsk_timer_enable(1)
+    try:
+        out = fn()
+        torch.cuda.synchronize()
+    finally:
+        lib.fsk_timer_enable(0)
+    rows = lib.fsk_timer_collect(ids.ctypes.data, nl.ctypes.data, ms.ctypes.data, work.ctypes.data, 16)
+    return out, {int(ids[r]) for r in range(rows)}
+
+
+SYMMETRIC_KERNELS = {4, 8}    # CUDA-core / tensor-core upper-triangle kernels
+ORDERED_KERNELS = {3, 7}
+
+
+@pytest.mark.parametrize("precision", ["tensor", "ieee"])
+def test_symmetric_matches_ordered_1024(cuda_dev, golden, precision):
     """tests/large/test_consistency_large.py:21-56 of the reference (tolerance
-    there 5e-3; here 1e-5)."""
+    there 5e-3; here 1e-5).  The two variants must run different kernels:
+    the symmetric one evaluates each pair's exp once (upper-triangle tiles)."""
     from fsk import ops
 
     g = golden("score16_seed10")
     x = torch.from_numpy(g["train"]).to(cuda_dev)
-    po, wo = ops.empscore16(x, 1.0, variant="ordered")
-    ps, wsym = ops.empscore16(x, 1.0, variant="symmetric")
+    (po, wo), ko = _kernel_ids(lambda: ops.empscore16(x, 1.0, variant="ordered", precision=precision))
+    (ps, wsym), ks = _kernel_ids(lambda: ops.empscore16(x, 1.0, variant="symmetric", precision=precision))
+    assert ko & ORDERED_KERNELS and not ko & SYMMETRIC_KERNELS
+    assert ks & SYMMETRIC_KERNELS and not ks & ORDERED_KERNELS
     _close(ps.cpu().numpy(), po.cpu().numpy())
     _close(wsym.cpu().numpy(), wo.cpu().numpy())
+    p64, w64, _ = fp64.empirical_score(g["train"], 1.0)
+    _close(ps.cpu().numpy(), p64, rtol=2e-6, floor=0)
+    _close(wsym.cpu().numpy(), w64, rtol=2e-6, floor=2e-6)
+
+
+@pytest.mark.parametrize("n", [1, 2, 63, 64, 65, 127, 128, 129, 255, 256, 257, 300, 513, 1000])
+def test_symmetric_tile_boundary_shapes(cuda_dev, n):
+    """Point counts around the triangle kernel's tiles (diagonal tiles,
+    ragged last tile): pdf and weighted sums vs the FP64 oracle."""
+    from fsk import ops
+
+    rng = np.random.default_rng(n + 29)
+    xs = (rng.standard_normal((n, 16)) * 1.5).astype(np.float32)
+    h = 0.8
+    pdf, w = ops.empscore16(torch.from_numpy(xs).to(cuda_dev), h, variant="symmetric")
+    ops.device_status(cuda_dev)
+    p64, w64, _ = fp64.empirical_score(xs, h)
+    _close(pdf.cpu().numpy(), p64, rtol=2e-6, floor=0)
+    _close(w.cpu().numpy(), w64, rtol=2e-6, floor=2e-6)
 
 
 def test_ordered_is_bitwise_deterministic(cuda_dev):
@@ -153,3 +199,57 @@ def test_score_offset_data(cuda_dev):
     assert rel_err(pdf.cpu().numpy(), p64).max() < 1e-5
     d64 = fp64.debias(xs, h)
     assert np.abs(deb.cpu().numpy() - d64).max() < 1e-5 * np.abs(d64).max()
+
+
+@pytest.mark.parametrize("return_tensor", [True, False])
+def test_empirical_sd_kde_triton_nd_vs_reference(cuda_dev, golden, return_tensor):
+    """kernels/flash_sd_kde/empirical.py:226-287 of the reference: the
+    debiased points (tensor or numpy) and the bandwidth it returns, against
+    the reference's outputs on the golden seeds and against FP64."""
+    from kernels.flash_sd_kde import empirical_sd_kde_triton_nd
+
+    for seed in (2, 3, 4, 10):
+        g = golden(f"score16_seed{seed}")
+        h = float(g["h"])
+        deb, h_out = empirical_sd_kde_triton_nd(g["train"], h, return_tensor=return_tensor)
+        assert h_out == h
+        if return_tensor:
+            assert isinstance(deb, torch.Tensor) and deb.is_cuda and deb.dtype == torch.float32
+            deb = deb.cpu().numpy()
+        else:
+            assert isinstance(deb, np.ndarray) and deb.dtype == np.float32
+        assert deb.shape == g["train"].shape
+        _close(deb, g["debiased"])
+        _close(deb, fp64.debias(g["train"], h), rtol=2e-6, floor=2e-6)
+
+
+@pytest.mark.parametrize("splits,count,features", [(1, 1, None), (7, 1000, None), (64, 4097, None),
+                                                    (5, 300, 16), (33, 129, 16), (1, 17, 3)])
+def test_reduce_partials_vs_fixed_order_fp64(cuda_dev, splits, count, features):
+    """kernels/reduce_partials.py:61-108 of the reference: the sum over the
+    split axis of (splits, n) and (splits, n, features) FP32 partials.  Here
+    the sum is formed in FP64 in split order, so it equals the FP64
+    fixed-order sum rounded once to FP32."""
+    from kernels.reduce_partials import reduce_pdf_partials, reduce_weighted_partials
+
+    rng = np.random.default_rng(splits * 1000 + count)
+    shape = (splits, count) if features is None else (splits, count, features)
+    # magnitudes over many binades with cancelling signs: an FP32 running sum would differ
+    p = (rng.standard_normal(shape) * 10.0 ** rng.uniform(-3, 3, size=shape)).astype(np.float32)
+    pt = torch.from_numpy(p).to(cuda_dev)
+    out = reduce_pdf_partials(pt) if features is None else reduce_weighted_partials(pt)
+    ops_out = out.cpu().numpy()
+    ref = np.zeros(shape[1:], np.float64)
+    for s in range(splits):
+        ref += p[s].astype(np.float64)
+    assert ops_out.shape == ref.shape and ops_out.dtype == np.float32
+    np.testing.assert_array_equal(ops_out, ref.astype(np.float32))
+
+
+def test_reduce_partials_rejects_bad_shapes(cuda_dev):
+    from kernels.reduce_partials import reduce_pdf_partials, reduce_weighted_partials
+
+    with pytest.raises(ValueError):
+        reduce_pdf_partials(torch.zeros((2, 3, 4), device=cuda_dev))
+    with pytest.raises(ValueError):
+        reduce_weighted_partials(torch.zeros((2, 3), device=cuda_dev))

@@ -69,3 +69,29 @@ def test_fp64_laplace_matches_fp32_oracle(golden):
     g = golden("kde16_lin_seed5")
     d64 = fp64.density(g["train"], g["queries"], float(g["h"]), laplace=True)
     np.testing.assert_allclose(d64, np.abs(g["density"]), rtol=1e-4)
+
+
+def test_fp64_gemm_oracle_matches_direct_differences():
+    """The FP64 expansion-about-the-mean oracle used at full sizes agrees with
+    the direct-difference FP64 oracle on offset heavy-tailed data (the
+    cancellation-stress distribution) to ~1e-11 in log p."""
+    from fsk import workloads
+
+    x = workloads.student_t_16d(6000, seed=4)
+    q = workloads.student_t_16d(200, seed=5)
+    for h in (0.3, 1.0, 3.0):
+        a = fp64.log_density(x, q, h)
+        b = fp64.log_density_gemm(x, q, h, s_chunk=1000, q_chunk=64, threads=2)
+        ok = np.isfinite(a)
+        assert ok.all() == np.isfinite(b).all()
+        assert np.abs(a[ok] - b[ok]).max() < 1e-10
+
+
+def test_log_error_metrics():
+    ref = np.array([-1.0, -2.0, -3.0, -np.inf])
+    got = np.array([-1.0 + 1e-6, -2.0 - 2e-6, -3.0, -5.0])
+    m = fp64.log_error_metrics(got, ref)
+    assert m["finite_fraction"] == 1.0 and m["finite_fraction_ref"] == 0.75
+    assert abs(m["max_abs_log_err"] - 2e-6) < 1e-12
+    assert abs(m["mean_abs_log_err"] - 1e-6) < 1e-12
+    assert abs(m["bias_log_err"] - (-1e-6 / 3)) < 1e-12
