@@ -89,7 +89,8 @@ def parse():
     ap.add_argument("--sur-train", type=int, default=262144, help="surrogate workload: exact SD-KDE fit points")
     ap.add_argument("--sur-pairs", type=int, default=4_000_000, help="surrogate workload: training pairs")
     ap.add_argument("--sur-eval", type=int, default=1_000_000, help="surrogate workload: held-out queries")
-    ap.add_argument("--op", choices=["kde16", "kde16_logexact", "score16", "score16_sym", "kde1d", "precision"],
+    ap.add_argument("--op", choices=["kde16", "kde16_offload", "kde16_logexact", "score16", "score16_sym", "kde1d",
+                                     "precision"],
                     default=None,
                     help="time one operation alone on n GMM8 points (profiling case; no contract line)")
     return ap.parse_args()
@@ -662,6 +663,16 @@ def surrogate_workload(args, dev) -> dict:
     rel = (torch.exp((logp - exact).double()) - 1).abs()
     srv = served.bool() & fin
     nq = q.shape[0]
+    # gate frontier: served fraction and served error as the ensemble-spread tolerance varies
+    mean_s, spread_s, _ = sur.predict(q)
+    in_r = sur._radius2(q) <= sur.r2_max_
+    rel_s = (torch.exp((mean_s - exact).double()) - 1).abs()
+    frontier = []
+    for tol in (0.005, 0.01, 0.02, 0.03, 0.05, 0.1, 0.2, float("inf")):
+        sel = (spread_s <= tol) & in_r & fin
+        frontier.append({"spread_tol": tol, "served_fraction": float(sel.float().mean()),
+                         "served_fraction_in_support": float(sel[:half].float().mean()),
+                         "median_rel_density_err_served": float(rel_s[sel].median()) if sel.any() else None})
     return {
         "workload": f"surrogate_gmm8_16d_fit{args.sur_train}_pairs{args.sur_pairs}_eval{nq}",
         "members": 4, "mlp": "16-256-256-256-1 SiLU, bf16 weights/activations, FP32 accumulation",
@@ -682,6 +693,7 @@ def surrogate_workload(args, dev) -> dict:
         "exact_recomputed_underflow_queries": recomputed,
         "exact_nonfinite_queries": int((~fin).sum()),
         "spread_tol": sur.spread_tol, "r2_max": sur.r2_max_,
+        "gate_frontier": frontier,
     }
 
 
@@ -782,6 +794,8 @@ def run_op(args) -> None:
     pairs = float(args.n) * args.n
     if args.op == "kde16":
         fn = lambda: ops.kde16_sum(x, x, h)
+    elif args.op == "kde16_offload":
+        fn = lambda: ops.kde16_sum(x, x, h, exp_offload=True)
     elif args.op == "kde16_logexact":
         q = x.clone()
         q[::2] += 60.0 * h / 4.0      # offset 15 h per feature: 60 h away in 16-D

@@ -82,7 +82,7 @@ size_t kde16_bytes(int64_t m, int64_t n, const Kde16Plan& p) {
 }
 
 constexpr int KNOWN_FLAGS = FSK_PREC_IEEE | FSK_LAPLACE | FSK_OUT_LOG | FSK_ATOMIC | FSK_WEIGHTED_FEATURE_MAJOR |
-                            FSK_OUT_LOG_EXACT | FSK_PREC_FP16_SINGLE;
+                            FSK_OUT_LOG_EXACT | FSK_PREC_FP16_SINGLE | FSK_EXP_OFFLOAD;
 
 // FSK_OUT_LOG_EXACT: only with FSK_OUT_LOG, out_eps = 0 and m < 2^32 (list indices)
 bool bad_log_exact(int flags, double out_eps, int64_t m) {
@@ -168,7 +168,7 @@ int fsk_kde16(const float* queries, int64_t m, const float* data, int64_t n, dou
   } else {
     launch_mean16(data, n, cb.scratch, cb.mu, cb.mu64, s);
     st = tc::launch_kde16_tc(queries, m, data, n, cb.mu, bandwidth, laplace, (flags & FSK_PREC_FP16_SINGLE) != 0,
-                             p.tcp, c, &part, p.atomic, s);
+                             (flags & FSK_EXP_OFFLOAD) != 0, p.tcp, c, &part, p.atomic, s);
     if (st) return st;
     splits = p.atomic ? 1 : (int)p.tcp.part_rows;
   }
@@ -217,7 +217,7 @@ int fsk_empscore16(const float* data, int64_t n, double bandwidth, int variant, 
                    float* weighted_sum, void* workspace, size_t workspace_bytes, void* stream) {
   if (!data || !pdf_sum || !weighted_sum || n < 1 || bad_bw(bandwidth)) return FSK_ERR_INVALID_ARGUMENT;
   if (variant != FSK_SCORE_ORDERED && variant != FSK_SCORE_SYMMETRIC) return FSK_ERR_INVALID_ARGUMENT;
-  if (flags & ~(KNOWN_FLAGS & ~FSK_PREC_FP16_SINGLE)) return FSK_ERR_INVALID_ARGUMENT;
+  if (flags & ~(KNOWN_FLAGS & ~(FSK_PREC_FP16_SINGLE | FSK_EXP_OFFLOAD))) return FSK_ERR_INVALID_ARGUMENT;
   int st = check_device();
   if (st) return st;
   cudaStream_t s = static_cast<cudaStream_t>(stream);

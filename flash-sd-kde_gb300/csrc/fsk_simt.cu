@@ -17,7 +17,6 @@
 // (four FMA chains joined pairwise) and the exponent product dist * log2(e)/(2h^2)
 // is carried in double-float (exp2_neg_scaled), so no step needs centring.
 #include "fsk_common.cuh"
-#include <type_traits>
 
 #include "fsk_kernels.cuh"
 
@@ -357,10 +356,10 @@ constexpr int K1_T = 1024;
 
 // Visits the valid points r0 .. rend-1 of a staged tile in order: four at a
 // time (one 16-byte shared load) for a full 32-point group, else one by one.
-// f(x, poly): poly (a compile-time constant) marks the points whose last query
-// pair takes the FMA-pipe exp2 instead of ex2.approx: every other point of a
-// full group (an eighth of the exps), where the exp pipe is the bound and the
-// issue slots have room; the ragged tail uses the exp pipe only.
+// (The exp stays on the exp pipe here: per pair the kernel also issues four
+// FP32 lane operations, so the FP32 pipe is as busy as the exp pipe and the
+// FMA-pipe exp2 would only move the bound: measured 6.6e12 vs 8.3e12 pair
+// evaluations per second with an eighth of the exps moved.)
 template <typename F>
 __device__ __forceinline__ void for_points(const float* xs, int r0, int rend, F&& f) {
   if (rend - r0 == 32) {
@@ -368,22 +367,14 @@ __device__ __forceinline__ void for_points(const float* xs, int r0, int rend, F&
 #pragma unroll 2
     for (int k = 0; k < 8; ++k) {
       const float4 v = xs4[k];
-      f(v.x, std::true_type{});
-      f(v.y, std::false_type{});
-      f(v.z, std::true_type{});
-      f(v.w, std::false_type{});
+      f(v.x);
+      f(v.y);
+      f(v.z);
+      f(v.w);
     }
   } else {
-    for (int r = r0; r < rend; ++r) f(xs[r], std::false_type{});
+    for (int r = r0; r < rend; ++r) f(xs[r]);
   }
-}
-
-// 2^a for the query pair p of a point: the exp pipe, or the FMA-pipe
-// polynomial for the last pair on the points for_points marks.
-template <typename Poly>
-__device__ __forceinline__ float2 exp2_pair(float2 a, int p, Poly) {
-  if (Poly::value && p == K1_P - 1) return exp2_poly2(a);
-  return make_float2(ex2_approx(a.x), ex2_approx(a.y));
 }
 }  // namespace
 
@@ -418,14 +409,14 @@ __global__ void __launch_bounds__(K1_THREADS) kde1d_kernel(
       float2 part[K1_P];
 #pragma unroll
       for (int p = 0; p < K1_P; ++p) part[p] = make_float2(0.f, 0.f);
-      for_points(xs, r0, min(valid, r0 + 32), [&](float xv, auto poly) {
+      for_points(xs, r0, min(valid, r0 + 32), [&](float xv) {
         const float2 x2 = make_float2(xv, xv);
 #pragma unroll
         for (int p = 0; p < K1_P; ++p) {
           const float2 d = __fadd2_rn(x2, nq[p]);
           const float2 t2 = __fmul2_rn(d, d);
           const float2 a = __fmul2_rn(t2, nc2_2);
-          float2 e = exp2_pair(a, p, poly);
+          float2 e = make_float2(ex2_approx(a.x), ex2_approx(a.y));
           if (LAPLACE) e = __fmul2_rn(e, __ffma2_rn(mc1_2, t2, c15_2));
           part[p] = __fadd2_rn(part[p], e);
         }
@@ -499,13 +490,13 @@ __global__ void __launch_bounds__(K1_THREADS) kde1d_score_kernel(
       float2 s0[K1_P], s1[K1_P];
 #pragma unroll
       for (int p = 0; p < K1_P; ++p) { s0[p] = make_float2(0.f, 0.f); s1[p] = make_float2(0.f, 0.f); }
-      for_points(xs, r0, min(valid, r0 + 32), [&](float xv, auto poly) {
+      for_points(xs, r0, min(valid, r0 + 32), [&](float xv) {
         const float2 x2 = make_float2(xv, xv);
 #pragma unroll
         for (int p = 0; p < K1_P; ++p) {
           const float2 d = __fadd2_rn(x2, nq[p]);    // x - q
           const float2 a = __fmul2_rn(__fmul2_rn(d, d), nc2_2);
-          const float2 e = exp2_pair(a, p, poly);
+          const float2 e = make_float2(ex2_approx(a.x), ex2_approx(a.y));
           s0[p] = __fadd2_rn(s0[p], e);
           s1[p] = __ffma2_rn(d, e, s1[p]);
         }

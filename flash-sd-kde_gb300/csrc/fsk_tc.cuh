@@ -112,8 +112,8 @@ __global__ void prep_query_kernel(const float* __restrict__ q, int64_t m, int64_
                                   float* __restrict__ qexact);
 size_t tc_kde16_ws_bytes(const TcPlan& pl, int64_t m, bool atomic);
 int launch_kde16_tc(const float* q, int64_t m, const float* x, int64_t n, const float* mu, double h,
-                    bool laplace, bool single, const TcPlan& pl, WsCarver& c, double** partials_out, bool atomic,
-                    cudaStream_t s);
+                    bool laplace, bool single, bool poly, const TcPlan& pl, WsCarver& c, double** partials_out,
+                    bool atomic, cudaStream_t s);
 TcPlan plan_score16(int64_t n);
 size_t tc_score16_ws_bytes(const TcPlan& pl, int64_t n);
 // Empirical-score partials: ppdf [2 * splits][n], pw [splits][n][16] (centred).

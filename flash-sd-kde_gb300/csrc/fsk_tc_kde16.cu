@@ -57,7 +57,11 @@ namespace tc {
 // SINGLE: the single-pass precision rung (FSK_PREC_FP16_SINGLE) - only the
 // hi.hi cross product (one fp16 product per feature, FP32 accumulation) and
 // the bias step, no exact near-pair recompute.
-template <bool LAPLACE, bool SINGLE>
+// POLY: the last POLY_COLS columns of every 32-column chunk take the FMA-pipe
+// exp2 (exp2_poly2) instead of ex2.approx, moving a quarter of the exps off
+// the exp pipe (the FP32 pipe carries ~one lane operation per pair here).
+constexpr int POLY_COLS = 8;
+template <bool LAPLACE, bool SINGLE, bool POLY>
 __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* sA = smem_raw;                               // NQT query tiles: H | M | L
@@ -268,10 +272,19 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
             }
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
+              if (POLY && j >= 32 - POLY_COLS) continue;
               float v = ex2_approx(e[j]);
               // Laplace factor 1 + d/2 - dist/(2h^2) = 9 + a2 ln 2   (a2 = -c2 dist)
               if (LAPLACE) v *= fmaf(e[j], 0.69314718055994531f, 1.0f + 0.5f * FSK_D);
               e[j] = v;
+            }
+            if (POLY) {
+#pragma unroll
+              for (int j = 32 - POLY_COLS; j < 32; j += 2) {
+                const float2 v = exp2_poly2(make_float2(e[j], e[j + 1]));
+                e[j] = v.x;
+                e[j + 1] = v.y;
+              }
             }
             const int cvalid = valid - c * 32;   // valid columns of this chunk (may be <= 0 or > 32)
             if (cvalid < 32) {  // ragged last data tile: drop padding columns
@@ -550,18 +563,18 @@ size_t tc_kde16_ws_bytes(const TcPlan& pl, int64_t m, bool atomic) {
   return b;
 }
 
-template <bool LAPLACE, bool SINGLE>
+template <bool LAPLACE, bool SINGLE, bool POLY = false>
 static cudaError_t launch_kde16_tc_kernel(const TcPlan& pl, const TcParams& p, cudaStream_t s) {
-  const cudaError_t e = cudaFuncSetAttribute(kde16_tc_kernel<LAPLACE, SINGLE>,
+  const cudaError_t e = cudaFuncSetAttribute(kde16_tc_kernel<LAPLACE, SINGLE, POLY>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
   if (e != cudaSuccess) return e;
-  kde16_tc_kernel<LAPLACE, SINGLE><<<pl.grid, THREADS, SMEM_BYTES, s>>>(p);
+  kde16_tc_kernel<LAPLACE, SINGLE, POLY><<<pl.grid, THREADS, SMEM_BYTES, s>>>(p);
   return cudaGetLastError();
 }
 
 int launch_kde16_tc(const float* q, int64_t m, const float* x, int64_t n, const float* mu, double h,
-                    bool laplace, bool single, const TcPlan& pl, WsCarver& c, double** partials_out, bool atomic,
-                    cudaStream_t s) {
+                    bool laplace, bool single, bool poly, const TcPlan& pl, WsCarver& c, double** partials_out,
+                    bool atomic, cudaStream_t s) {
   TcScales* sc = c.take<TcScales>(1);
   uint8_t* qimg = c.take<uint8_t>((size_t)pl.q_blocks * A_BYTES);
   float* qexact = c.take<float>((size_t)pl.m_pad * FSK_D);
@@ -610,8 +623,10 @@ int launch_kde16_tc(const float* q, int64_t m, const float* x, int64_t n, const 
   TimerScope ts(K_KDE16_TC, (double)m * (double)n, s);
   if (laplace)
     e = single ? launch_kde16_tc_kernel<true, true>(pl, p, s) : launch_kde16_tc_kernel<true, false>(pl, p, s);
+  else if (single)
+    e = launch_kde16_tc_kernel<false, true>(pl, p, s);
   else
-    e = single ? launch_kde16_tc_kernel<false, true>(pl, p, s) : launch_kde16_tc_kernel<false, false>(pl, p, s);
+    e = poly ? launch_kde16_tc_kernel<false, false, true>(pl, p, s) : launch_kde16_tc_kernel<false, false>(pl, p, s);
   count_launch();
   return cuda_status(e);
 }

@@ -30,6 +30,7 @@ FSK_ATOMIC = 0x8
 FSK_WEIGHTED_FEATURE_MAJOR = 0x10
 FSK_OUT_LOG_EXACT = 0x20
 FSK_PREC_FP16_SINGLE = 0x40
+FSK_EXP_OFFLOAD = 0x80
 
 FSK_ND_MAX = 64
 FSK_NOALLOC_SCRATCH_BYTES = 32 << 20

@@ -99,6 +99,7 @@ def kde16_sum(
     log_eps: float | None = None,
     log_exact: bool = False,
     out: torch.Tensor | None = None,
+    exp_offload: bool = False,
 ) -> torch.Tensor:
     """out[i] = out_scale * sum_j phi(q_i, x_j)  (or log(out_scale*sum + log_eps)).
 
@@ -121,6 +122,7 @@ def kde16_sum(
         raise ValueError(f"unknown precision {precision!r}")
     flags = {"tensor": L.FSK_PREC_TENSOR, "ieee": L.FSK_PREC_IEEE, "fp16_single": L.FSK_PREC_FP16_SINGLE}[precision]
     flags |= (L.FSK_LAPLACE if laplace else 0) | (L.FSK_ATOMIC if atomic else 0)
+    flags |= L.FSK_EXP_OFFLOAD if exp_offload else 0
     if log_exact:
         if log_eps:
             raise ValueError("log_exact takes no log_eps (the log is taken without a floor).")

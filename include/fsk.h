@@ -74,6 +74,10 @@ enum fsk_status {
  * (FP32 accumulation; the norms keep their three-part precision), no exact
  * near-pair recompute.  For precision studies; not an exact mode. */
 #define FSK_PREC_FP16_SINGLE 0x40
+/* fsk_kde16 tensor precision only: a quarter of the exps on the FP32 FMA pipe
+ * (degree-5 Remez polynomial for 2^r with exponent-field insertion, about
+ * the error of ex2.approx.f32) instead of the exp pipe. */
+#define FSK_EXP_OFFLOAD 0x80
 /* Laplace-corrected ("linearized") kernel phi * (1 + d/2 - dist/(2 h^2)),
  * kernels/kde_eval_16d_stream_splitk.py:75-76. */
 #define FSK_LAPLACE 0x2

@@ -273,3 +273,46 @@ def test_kde_eval_log_eps0_and_estimator_log_space(cuda_dev):
     far = ref < -200.0
     assert far.any() and np.allclose(floor[far], np.log(1e-12), rtol=0, atol=1e-5)
 
+
+
+@pytest.mark.parametrize("name", ["kde16_plain_4096x1024", "kde16_seed1", "kde16_seed11"])
+def test_exp_offload_vs_reference_and_fp64(cuda_dev, golden, name):
+    """FSK_EXP_OFFLOAD: a quarter of the exps by the FMA-pipe polynomial
+    (exp2_poly2) instead of ex2.approx; the same bars as the default tensor
+    path against the reference outputs and FP64, and within 1e-6 of it."""
+    g = golden(name)
+    h = float(g["h"])
+    out = _kde(cuda_dev, g["queries"], g["train"], h, "tensor", exp_offload=True)
+    base = _kde(cuda_dev, g["queries"], g["train"], h, "tensor")
+    assert rel_err(out, g["density"]).max() < 1e-5
+    assert rel_err(out, base).max() < 1e-6
+    if "log_density_fp64" in g:
+        e64 = rel_err(out, np.exp(g["log_density_fp64"]))
+        assert e64.max() < 1e-5 and np.median(e64) < 1e-6, (e64.max(), np.median(e64))
+
+
+def test_exp_offload_far_queries_and_flags(cuda_dev):
+    """Queries far from the data: where the unnormalised sum is above
+    n 2^-100 (so terms below FP32's 2^-126, which ex2.approx flushes and the
+    polynomial clamps to ~2^-125, cannot move it by 1e-6) the densities agree
+    to 1e-6; below that both are negligible.  The offload flag is refused
+    outside fsk_kde16's tensor path."""
+    from fsk import _lib as L
+
+    rng = np.random.default_rng(3)
+    n = 3000
+    x = rng.standard_normal((n, 16)).astype(np.float32)
+    q = np.concatenate([rng.standard_normal((200, 16)), rng.standard_normal((56, 16)) + 4.0]).astype(np.float32)
+    for h in (0.3, 0.8):
+        out = _kde(cuda_dev, q, x, h, "tensor", exp_offload=True, scale=1.0)
+        base = _kde(cuda_dev, q, x, h, "tensor", scale=1.0)
+        big = base > n * 2.0 ** -100
+        assert big.sum() > 150
+        assert rel_err(out[big], base[big]).max() < 1e-6
+        assert (out[~big] <= 2.0 * n * 2.0 ** -100).all()
+    lib = L.load()
+    t = torch.zeros((4, 16), device=cuda_dev)
+    pdf = torch.zeros(4, device=cuda_dev)
+    st = lib.fsk_empscore16(t.data_ptr(), 4, 1.0, 0, L.FSK_EXP_OFFLOAD, pdf.data_ptr(), t.data_ptr(), None, 0,
+                            torch.cuda.current_stream().cuda_stream)
+    assert st == L.FSK_ERR_INVALID_ARGUMENT
