@@ -90,7 +90,7 @@ def parse():
     ap.add_argument("--sur-pairs", type=int, default=4_000_000, help="surrogate workload: training pairs")
     ap.add_argument("--sur-eval", type=int, default=1_000_000, help="surrogate workload: held-out queries")
     ap.add_argument("--op", choices=["kde16", "kde16_offload", "kde16_logexact", "score16", "score16_sym", "kde1d",
-                                     "precision"],
+                                     "precision", "sdkde_latency"],
                     default=None,
                     help="time one operation alone on n GMM8 points (profiling case; no contract line)")
     return ap.parse_args()
@@ -759,6 +759,54 @@ def run_precision(args) -> None:
                       "queries_checked": int(sub.size), "silverman_h": h0, "rows": rows}), flush=True)
 
 
+def run_sdkde_latency(args) -> None:
+    """Per-call time of the whole SD-KDE step (score + debias + KDE) at small
+    sizes, where launch overhead matters: the public two-call path
+    (emp_sd_kde_fit_transform + kde_eval), the one-call fsk_sdkde16, and that
+    call replayed from a captured CUDA graph.  Sizes: 4096 train / 1024
+    queries (the plain-KDE configuration's shape) and 65536 / 65536."""
+    import torch
+
+    import __graft_entry__ as ge
+
+    ge.build()
+    from flash_sd_kde import emp_sd_kde_fit_transform, kde_eval
+    from fsk import ops, workloads
+
+    dev = torch.device("cuda", 0)
+    rows = []
+    for n, m in ((4096, 1024), (16384, 4096), (65536, 65536)):
+        g = workloads.GMM16(seed=0)
+        x = torch.from_numpy(g.sample(n, seed=1)).to(dev)
+        q = torch.from_numpy(g.sample(m, seed=2)).to(dev)
+        h = float(ops.silverman(x).item())
+        graph = ops.SDKDEGraph(x, q, h)
+        ws = ops._workspace(ops.L.load().fsk_sdkde16_workspace_bytes(n, m, 0), dev)
+        out = torch.empty(m, dtype=torch.float32, device=dev)
+        fns = {"two_calls": lambda: kde_eval(emp_sd_kde_fit_transform(x, h, device=dev), q, h, device=dev),
+               "one_call": lambda: ops.sdkde16(x, q, h, out=out, workspace=ws),
+               "graph_replay": graph.replay}
+        row = {"n_train": n, "n_query": m}
+        for name, fn in fns.items():
+            for _ in range(max(3, args.warmup)):
+                fn()
+            torch.cuda.synchronize(dev)
+            reps = max(10, args.steps)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            t0 = time.perf_counter()
+            e0.record()
+            for _ in range(reps):
+                fn()
+            e1.record()
+            torch.cuda.synchronize(dev)
+            row[name + "_us"] = 1e3 * e0.elapsed_time(e1) / reps
+            row[name + "_host_us"] = 1e6 * (time.perf_counter() - t0) / reps
+        ops.device_status(dev)
+        rows.append(row)
+        print(json.dumps(row), file=sys.stderr, flush=True)
+    print(json.dumps({"op": "sdkde_latency", "rows": rows}), flush=True)
+
+
 def run_op(args) -> None:
     """One operation alone (the profiling case for ncu captures): n GMM8
     points as data and as queries, Silverman bandwidth, W warm-up and K timed
@@ -774,6 +822,8 @@ def run_op(args) -> None:
 
     if args.op == "precision":
         return run_precision(args)
+    if args.op == "sdkde_latency":
+        return run_sdkde_latency(args)
     ge.build()
     from fsk import ops, workloads
 

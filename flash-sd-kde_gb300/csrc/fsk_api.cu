@@ -265,6 +265,57 @@ int fsk_debias16(const float* data, int64_t n, const float* pdf_sum, const float
   return cuda_status(cudaGetLastError());
 }
 
+// ---- one-call SD-KDE: score -> debias -> KDE --------------------------------------
+// Workspace: pdf_sum (n) | weighted_sum (n, 16) | debiased (n, 16) unless the
+// caller takes it | the larger of the score and KDE workspaces (they run one
+// after the other on the stream and share it).
+static const int kSdkdeScoreFlags = FSK_PREC_IEEE;
+static const int kSdkdeKdeFlags = FSK_PREC_IEEE | FSK_OUT_LOG | FSK_OUT_LOG_EXACT | FSK_ATOMIC;
+
+static size_t sdkde_bytes(int64_t n, int64_t m, int flags) {
+  WsCarver c(nullptr, 0);
+  c.take<float>((size_t)n);
+  c.take<float>((size_t)n * FSK_D);
+  c.take<float>((size_t)n * FSK_D);
+  const size_t a = fsk_empscore16_workspace_bytes(n, FSK_SCORE_ORDERED, flags & kSdkdeScoreFlags);
+  const size_t b = fsk_kde16_workspace_bytes(m, n, flags & kSdkdeKdeFlags);
+  c.used = align_up(c.used, 256) + (a > b ? a : b);
+  return align_up(c.used, 256);
+}
+
+size_t fsk_sdkde16_workspace_bytes(int64_t n, int64_t m, int flags) {
+  if (n < 1 || m < 1) return 0;
+  return sdkde_bytes(n, m, flags);
+}
+
+int fsk_sdkde16(const float* data, int64_t n, const float* queries, int64_t m, double bandwidth, int flags,
+                double eps, double out_scale, double out_eps, float* debiased, float* out, void* workspace,
+                size_t workspace_bytes, void* stream) {
+  if (!data || !queries || !out || n < 1 || m < 1 || bad_bw(bandwidth) || !(eps >= 0.0))
+    return FSK_ERR_INVALID_ARGUMENT;
+  if (flags & ~kSdkdeKdeFlags) return FSK_ERR_INVALID_ARGUMENT;
+  int st = validate_kde16_args(queries, m, data, n, bandwidth, flags & kSdkdeKdeFlags, out_eps, out);
+  if (st) return st;
+  st = check_device();
+  if (st) return st;
+  if (!workspace || workspace_bytes < sdkde_bytes(n, m, flags)) return FSK_ERR_WORKSPACE_TOO_SMALL;
+  WsCarver c(workspace, workspace_bytes);
+  float* pdf = c.take<float>((size_t)n);
+  float* w = c.take<float>((size_t)n * FSK_D);
+  float* deb_ws = c.take<float>((size_t)n * FSK_D);
+  float* deb = debiased ? debiased : deb_ws;
+  c.used = align_up(c.used, 256);
+  void* rest = static_cast<char*>(workspace) + c.used;
+  const size_t rest_bytes = workspace_bytes - c.used;
+  st = fsk_empscore16(data, n, bandwidth, FSK_SCORE_ORDERED, flags & kSdkdeScoreFlags, pdf, w, rest, rest_bytes,
+                      stream);
+  if (st) return st;
+  st = fsk_debias16(data, n, pdf, w, FSK_D, 1, bandwidth, eps, deb, nullptr, stream);
+  if (st) return st;
+  return fsk_kde16(queries, m, deb, n, bandwidth, flags & kSdkdeKdeFlags, out_scale, out_eps, out, rest, rest_bytes,
+                   stream);
+}
+
 // ---- any d <= FSK_ND_MAX (CUDA cores) ------------------------------------------------
 size_t fsk_kde_nd_workspace_bytes(int64_t m, int64_t n, int d, int flags) {
   (void)flags;

@@ -242,3 +242,30 @@ def emp_sd_kde_fit_transform(
         return debiased, pdf_sum, weighted_sum, score
     debiased = ops.debias16(train, pdf_sum, weighted_sum, bandwidth, eps)
     return debiased[:, :d].contiguous() if d < ND_FEATURES else debiased
+
+
+def sd_kde_eval(
+    data,
+    queries,
+    bandwidth: float,
+    *,
+    device: str | torch.device = "cuda",
+    precision_mode: str = DEFAULT_PRECISION_MODE,
+    eps: float = DEFAULT_EPS,
+    return_debiased: bool = False,
+):
+    """One-step empirical SD-KDE of `data` evaluated at `queries` in one
+    library call: the same values as
+    kde_eval(emp_sd_kde_fit_transform(data, h, emp_score_backend="ordered_splitk"), queries, h)
+    (the reference runs these as two calls; flash_sd_kde/kde.py:49, :258).
+    16-D inputs only."""
+    if bandwidth <= 0:
+        raise ValueError("bandwidth must be positive.")
+    validate_precision_mode(precision_mode)
+    device = _require_cuda(device, "sd_kde_eval")
+    train = ops.as_matrix(data, device, ND_FEATURES)
+    query = ops.as_matrix(queries, device, ND_FEATURES)
+    if train.shape[0] == 0 or query.shape[0] == 0:
+        raise ValueError("data and queries must be non-empty.")
+    prec = "ieee" if precision_mode == PRECISION_FP32_IEEE else "tensor"
+    return ops.sdkde16(train, query, bandwidth, precision=prec, eps=eps, return_debiased=return_debiased)

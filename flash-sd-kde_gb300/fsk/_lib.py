@@ -65,6 +65,8 @@ SIGNATURES: dict[str, tuple] = {
     "fsk_empscore16_workspace_bytes": (_sz, [_i64, _int, _int]),
     "fsk_empscore16": (_int, [_vp, _i64, _d, _int, _int, _vp, _vp, _vp, _sz, _vp]),
     "fsk_debias16": (_int, [_vp, _i64, _vp, _vp, _i64, _i64, _d, _d, _vp, _vp, _vp]),
+    "fsk_sdkde16_workspace_bytes": (_sz, [_i64, _i64, _int]),
+    "fsk_sdkde16": (_int, [_vp, _i64, _vp, _i64, _d, _int, _d, _d, _d, _vp, _vp, _vp, _sz, _vp]),
     "fsk_kde1d_workspace_bytes": (_sz, [_i64, _i64, _int]),
     "fsk_kde1d": (_int, [_vp, _i64, _vp, _i64, _d, _int, _d, _d, _vp, _vp, _sz, _vp]),
     "fsk_kde1d_score": (_int, [_vp, _i64, _vp, _i64, _d, _vp, _vp, _vp, _vp, _sz, _vp]),

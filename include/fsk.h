@@ -168,6 +168,23 @@ FSK_API int fsk_empscore16(const float* data, int64_t n, double bandwidth, int v
                    int flags, float* pdf_sum, float* weighted_sum,
                    void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---- SD-KDE in one call: score -> debias -> KDE ----------------------- */
+/* The pipeline the reference runs as empirical_sd_kde_triton_nd followed by
+ * gaussian_kde_triton_nd (experiments/runtime/benchmark_triton_kde.py:344-388,
+ * kernels/flash_sd_kde/empirical.py:226, kernels/flash_sd_kde/kde.py:242) or
+ * emp_sd_kde_fit_transform followed by kde_eval (flash_sd_kde/kde.py:258, :49),
+ * enqueued by one call on one workspace: the ordered empirical score of the
+ * data, the debias shift (eps on the unnormalised pdf_sum, as fsk_debias16)
+ * and the 16-D KDE of the debiased set at the queries (out as fsk_kde16).
+ * flags: FSK_PREC_IEEE (both stages), FSK_ATOMIC, FSK_OUT_LOG,
+ * FSK_OUT_LOG_EXACT (KDE stage).  debiased (n, 16) may be NULL.  No
+ * allocation and no synchronisation, so the call can be captured into a
+ * CUDA graph and replayed as one launch. */
+FSK_API size_t fsk_sdkde16_workspace_bytes(int64_t n, int64_t m, int flags);
+FSK_API int fsk_sdkde16(const float* data, int64_t n, const float* queries, int64_t m, double bandwidth,
+                        int flags, double eps, double out_scale, double out_eps, float* debiased, float* out,
+                        void* workspace, size_t workspace_bytes, void* stream);
+
 /* ---- one-step SD-KDE debias shift -------------------------------------- */
 /* score = (W / (pdf + eps) - x) / h^2, debiased = x + h^2/2 * score, in FP64.
  * weighted_sum element (i, k) is read at weighted_sum[i*w_row_stride + k*w_col_stride].

@@ -253,3 +253,39 @@ def test_reduce_partials_rejects_bad_shapes(cuda_dev):
         reduce_pdf_partials(torch.zeros((2, 3, 4), device=cuda_dev))
     with pytest.raises(ValueError):
         reduce_weighted_partials(torch.zeros((2, 3), device=cuda_dev))
+
+
+@pytest.mark.parametrize("precision", ["tensor", "ieee"])
+def test_one_call_sdkde_matches_two_calls_and_fp64(cuda_dev, precision):
+    """fsk_sdkde16 (score -> debias -> KDE in one call) gives bit for bit the
+    result of the public two-call path (emp_sd_kde_fit_transform with the
+    ordered backend, then kde_eval), matches the FP64 pipeline, and replays
+    identically from a captured CUDA graph."""
+    from flash_sd_kde import emp_sd_kde_fit_transform, kde_eval
+    from flash_sd_kde.kde import sd_kde_eval
+    from fsk import ops, workloads
+
+    g = workloads.GMM16(seed=0)
+    x_np, q_np = g.sample(3000, seed=1), g.sample(700, seed=2)
+    x = torch.from_numpy(x_np).to(cuda_dev)
+    q = torch.from_numpy(q_np).to(cuda_dev)
+    h = 0.7
+    mode = "fp32_ieee" if precision == "ieee" else "fast_tf32"
+    dens, deb = sd_kde_eval(x, q, h, precision_mode=mode, return_debiased=True)
+    deb2 = emp_sd_kde_fit_transform(x, h, precision_mode=mode, emp_score_backend="ordered_splitk")
+    dens2 = kde_eval(deb2, q, h, precision_mode=mode)
+    ops.device_status(cuda_dev)
+    assert torch.equal(deb, deb2) and torch.equal(dens, dens2)
+    deb64 = fp64.debias(x_np, h)
+    ref = np.exp(fp64.log_density(deb64, q_np, h))
+    assert rel_err(dens.cpu().numpy(), ref).max() < 1e-5
+    graph = ops.SDKDEGraph(x, q, h, precision=precision)
+    out = graph.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(out, dens)
+    # new inputs copied into the captured buffers
+    x_b = torch.from_numpy(g.sample(3000, seed=5)).to(cuda_dev)
+    graph.data.copy_(x_b)
+    out_b = graph.replay().clone()
+    ops.device_status(cuda_dev)
+    assert torch.equal(out_b, sd_kde_eval(x_b, q, h, precision_mode=mode))
