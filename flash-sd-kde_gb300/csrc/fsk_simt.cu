@@ -222,115 +222,131 @@ int simt_score16_splits(int64_t n) {
 }
 
 // ---------------------------------------------------------------------------
-// 16-D empirical score, symmetric.  One block per upper-triangle tile pair
-// (I <= J) of SYM_T rows; thread t owns row I*SYM_T + t.  Row sums are kept
-// in registers; column sums go through warp shuffles and shared FP32 into
-// FP64 atomics on the accumulators acc_pdf[n], acc_w[n][16].
+// 16-D empirical score, symmetric (phi_ij = phi_ji: each pair's exp once).
+// Block = one row tile I (SYM_T points, thread t owns row i = I*SYM_T + t)
+// against a run of up to SYM_L column tiles J >= I.  Per column tile:
+//   phase 1 (thread = row i): phi_ij for the tile's SYM_T points from direct
+//     FP32 differences of the original coordinates; the row sums pdf_i and
+//     W_i += phi_ij (x_j - mu) accumulate in registers (per-tile partials,
+//     then compensated across the run); phi_ij goes to shared memory;
+//   phase 2 (thread = column j = J*SYM_T + t): the column sums
+//     sum_i phi_ij and sum_i phi_ij (x_i - mu) from shared memory, added to
+//     the FP64 accumulators with atomics once per tile.
+// The row sums go to the FP64 accumulators once per run.  On the diagonal
+// tile (J == I) the row side takes j >= i (self pair included) and the
+// column side j > i, so every unordered pair and the self pair count once
+// per point.
 // ---------------------------------------------------------------------------
 namespace {
-constexpr int SYM_T = 64;
+constexpr int SYM_T = 64;   // points per tile (threads per block)
+constexpr int SYM_L = 16;   // column tiles per block
 }
 
 __global__ void __launch_bounds__(SYM_T) score16_sym_simt_kernel(
     const float* __restrict__ x, int64_t n, const float* __restrict__ mu, float c2, float c2_lo,
     int64_t n_tiles, double* __restrict__ acc_pdf, double* __restrict__ acc_w) {
-  // Map the linear block id to an upper-triangle pair (I, J), I <= J.
-  const int64_t b = blockIdx.x;
-  // row I has (n_tiles - I) pairs; find I by walking (n_tiles is moderate).
-  int64_t I = 0, rem = b;
-  {
-    // closed form start: solve I from cumulative counts.
-    double nt = (double)n_tiles;
-    double disc = (2.0 * nt + 1.0) * (2.0 * nt + 1.0) - 8.0 * (double)b;
-    int64_t guess = (int64_t)floor(((2.0 * nt + 1.0) - sqrt(fmax(disc, 0.0))) / 2.0);
-    guess = imax<int64_t>(0, imin<int64_t>(guess, n_tiles - 1));
-    auto start = [&](int64_t r) { return r * n_tiles - r * (r - 1) / 2; };
-    while (guess > 0 && start(guess) > b) --guess;
-    while (guess + 1 < n_tiles && start(guess + 1) <= b) ++guess;
-    I = guess;
-    rem = b - start(I);
-  }
-  const int64_t J = I + rem;
+  const int64_t I = blockIdx.x;
+  const int64_t J0 = I + (int64_t)blockIdx.y * SYM_L;
+  if (J0 >= n_tiles) return;   // beyond the end of this row tile's run (uniform per block)
+  const int64_t J1 = imin<int64_t>(n_tiles, J0 + SYM_L);
 
-  __shared__ __align__(16) float xj[SYM_T][FSK_D];
-  __shared__ float col_acc[SYM_T][FSK_D + 1];
+  __shared__ __align__(16) float xs[SYM_T][FSK_D];    // column tile, original coordinates
+  __shared__ __align__(16) float xcs[SYM_T][FSK_D];   // column tile, x - mu
+  __shared__ __align__(16) float xic[SYM_T][FSK_D];   // row tile, x - mu (phase 2)
+  __shared__ float phi[SYM_T][SYM_T + 1];              // [column][row], padded: conflict-free both ways
   __shared__ float mus[FSK_D];
-  if (threadIdx.x < FSK_D) mus[threadIdx.x] = mu[threadIdx.x];
+  const int t = threadIdx.x;
+  if (t < FSK_D) mus[t] = mu[t];
   __syncthreads();
-  const int64_t i = I * SYM_T + threadIdx.x;
+  const int64_t i = I * SYM_T + t;
   const bool vi = i < n;
-  float xi[FSK_D], xic[FSK_D];
+  float xi[FSK_D];
 #pragma unroll
   for (int k = 0; k < FSK_D; ++k) {
     xi[k] = vi ? x[i * FSK_D + k] : 0.f;
-    xic[k] = vi ? xi[k] - mus[k] : 0.f;
+    xic[t][k] = vi ? xi[k] - mus[k] : 0.f;
   }
-  const int64_t j0 = J * SYM_T;
-  const int validj = (int)imin<int64_t>(SYM_T, n - j0);
-  for (int e = threadIdx.x; e < SYM_T * FSK_D; e += SYM_T) {
-    int r = e / FSK_D, k = e % FSK_D;
-    xj[r][k] = r < validj ? x[(j0 + r) * FSK_D + k] : 0.f;
-  }
-  for (int e = threadIdx.x; e < SYM_T * (FSK_D + 1); e += SYM_T) (&col_acc[0][0])[e] = 0.f;
-  __syncthreads();
+  Comp prow{0.f, 0.f};
+  Comp wrow[FSK_D];
+#pragma unroll
+  for (int k = 0; k < FSK_D; ++k) wrow[k] = Comp{0.f, 0.f};
 
-  const bool diag = (I == J);
-  float prow = 0.f, wrow[FSK_D];
-#pragma unroll
-  for (int k = 0; k < FSK_D; ++k) wrow[k] = 0.f;
-  for (int r = 0; r < validj; ++r) {
-    float xv[FSK_D];
-#pragma unroll
-    for (int k = 0; k < FSK_D; k += 4) {
-      float4 v = *reinterpret_cast<const float4*>(&xj[r][k]);
-      xv[k] = v.x; xv[k + 1] = v.y; xv[k + 2] = v.z; xv[k + 3] = v.w;
+  for (int64_t J = J0; J < J1; ++J) {
+    const int64_t j0 = J * SYM_T;
+    const int validj = (int)imin<int64_t>(SYM_T, n - j0);
+    const bool diag = J == I;
+    __syncthreads();   // previous tile's phase 2 is done with phi / xs
+    for (int e = t; e < SYM_T * FSK_D; e += SYM_T) {
+      const int r = e / FSK_D, k = e % FSK_D;
+      const float v = r < validj ? x[(j0 + r) * FSK_D + k] : 0.f;
+      xs[r][k] = v;
+      xcs[r][k] = r < validj ? v - mus[k] : 0.f;
     }
-    const float e = exp2_neg_scaled(sqdist16(xi, xv), c2, c2_lo);
-    // row contribution: all (i, j) in the tile pair; on the diagonal tile only j >= i
-    float er = (vi && (!diag || r >= (int)threadIdx.x)) ? e : 0.f;
-    prow += er;
+    __syncthreads();
+    // phase 1: row i against the tile's points
+    float ps = 0.f, wp[FSK_D];
 #pragma unroll
-    for (int k = 0; k < FSK_D; ++k) wrow[k] = fmaf(er, xv[k] - mus[k], wrow[k]);
-    // column contribution (j receives phi_ij * x_i): off-diagonal pairs, or j > i on the diagonal
-    float ec = (vi && (!diag || r > (int)threadIdx.x)) ? e : 0.f;
-    float cv[FSK_D + 1];
-    cv[FSK_D] = ec;
+    for (int k = 0; k < FSK_D; ++k) wp[k] = 0.f;
+    for (int r = 0; r < SYM_T; ++r) {
+      float xv[FSK_D], xc[FSK_D];
 #pragma unroll
-    for (int k = 0; k < FSK_D; ++k) cv[k] = ec * xic[k];
+      for (int k = 0; k < FSK_D; k += 4) {
+        const float4 v = *reinterpret_cast<const float4*>(&xs[r][k]);
+        xv[k] = v.x; xv[k + 1] = v.y; xv[k + 2] = v.z; xv[k + 3] = v.w;
+        const float4 c = *reinterpret_cast<const float4*>(&xcs[r][k]);
+        xc[k] = c.x; xc[k + 1] = c.y; xc[k + 2] = c.z; xc[k + 3] = c.w;
+      }
+      const bool ok = vi && r < validj;
+      const float e = ok ? exp2_neg_scaled(sqdist16(xi, xv), c2, c2_lo) : 0.f;
+      const float er = (!diag || r >= t) ? e : 0.f;
+      ps += er;
 #pragma unroll
-    for (int k = 0; k <= FSK_D; ++k) {
-      float v = cv[k];
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-      cv[k] = v;
+      for (int k = 0; k < FSK_D; ++k) wp[k] = fmaf(er, xc[k], wp[k]);
+      phi[r][t] = (!diag || r > t) ? e : 0.f;
     }
-    if ((threadIdx.x & 31) == 0) {
+    prow.add(ps);
 #pragma unroll
-      for (int k = 0; k <= FSK_D; ++k) atomicAdd(&col_acc[r][k], cv[k]);
+    for (int k = 0; k < FSK_D; ++k) wrow[k].add(wp[k]);
+    __syncthreads();
+    // phase 2: column j = j0 + t against the row tile
+    if (t < validj) {
+      float pc = 0.f, wc[FSK_D];
+#pragma unroll
+      for (int k = 0; k < FSK_D; ++k) wc[k] = 0.f;
+      for (int r = 0; r < SYM_T; ++r) {
+        const float e = phi[t][r];
+#pragma unroll
+        for (int k = 0; k < FSK_D; k += 4) {
+          const float4 c = *reinterpret_cast<const float4*>(&xic[r][k]);
+          wc[k] = fmaf(e, c.x, wc[k]);
+          wc[k + 1] = fmaf(e, c.y, wc[k + 1]);
+          wc[k + 2] = fmaf(e, c.z, wc[k + 2]);
+          wc[k + 3] = fmaf(e, c.w, wc[k + 3]);
+        }
+        pc += e;
+      }
+      const int64_t j = j0 + t;
+      atomicAdd(&acc_pdf[j], (double)pc);
+#pragma unroll
+      for (int k = 0; k < FSK_D; ++k) atomicAdd(&acc_w[j * FSK_D + k], (double)wc[k]);
     }
   }
-  __syncthreads();
   if (vi) {
-    atomicAdd(&acc_pdf[i], (double)prow);
+    atomicAdd(&acc_pdf[i], (double)prow.s + (double)prow.c);
 #pragma unroll
-    for (int k = 0; k < FSK_D; ++k) atomicAdd(&acc_w[i * FSK_D + k], (double)wrow[k]);
-  }
-  if (threadIdx.x < validj) {
-    const int64_t j = j0 + threadIdx.x;
-    atomicAdd(&acc_pdf[j], (double)col_acc[threadIdx.x][FSK_D]);
-#pragma unroll
-    for (int k = 0; k < FSK_D; ++k) atomicAdd(&acc_w[j * FSK_D + k], (double)col_acc[threadIdx.x][k]);
+    for (int k = 0; k < FSK_D; ++k) atomicAdd(&acc_w[i * FSK_D + k], (double)wrow[k].s + (double)wrow[k].c);
   }
 }
 
 void launch_score16_sym_simt(const float* x, int64_t n, const float* mu, double h, double* acc_pdf,
                              double* acc_w, cudaStream_t s) {
   const int64_t n_tiles = (n + SYM_T - 1) / SYM_T;
-  const int64_t pairs = n_tiles * (n_tiles + 1) / 2;
   const double c2d = FSK_LOG2E / (2.0 * h * h);
   const float c2 = (float)c2d, c2_lo = (float)(c2d - (double)c2);
+  // grid.x: row tile; grid.y: run index (runs past the last tile exit at once)
+  const dim3 grid((unsigned)n_tiles, (unsigned)((n_tiles + SYM_L - 1) / SYM_L));
   TimerScope ts(K_SCORE16_SYM_SIMT, 0.5 * (double)n * (double)(n + 1), s);
-  score16_sym_simt_kernel<<<(unsigned)pairs, SYM_T, 0, s>>>(x, n, mu, c2, c2_lo, n_tiles, acc_pdf, acc_w);
+  score16_sym_simt_kernel<<<grid, SYM_T, 0, s>>>(x, n, mu, c2, c2_lo, n_tiles, acc_pdf, acc_w);
   count_launch();
 }
 

@@ -69,10 +69,14 @@ def test_precision_stress_2p20_offset_student_t(cuda_dev):
 
 
 def test_score_2p22_rows_and_determinism(cuda_dev):
-    """n = 2^22 = 4 194 304 anisotropic points: the ordered tensor-core score
-    is bitwise identical across two runs, and rows across the whole range
-    (including those past 64 * 65535 = 4 194 240, where the reference's flash
-    kernel writes the wrong rows) match the FP64 oracle."""
+    """n = 2^22 = 4 194 304 anisotropic points (the large low-rank
+    configuration): the ordered tensor-core score is bitwise identical across
+    two runs, rows across the whole range (including those past
+    64 * 65535 = 4 194 240, where the reference's flash kernel writes the
+    wrong rows) match the FP64 oracle, and the symmetric variant agrees with
+    the ordered one on every row (the reference cannot run either variant
+    here: its symmetric grid needs 65 536 > 65 535 blocks in y, its ordered
+    partials ~1.1 TB)."""
     from fsk import ops, workloads
 
     n = 1 << 22
@@ -89,6 +93,16 @@ def test_score_2p22_rows_and_determinism(cuda_dev):
     w = w1.cpu().numpy()[rows]
     assert rel_err(pdf, p64).max() < 1e-5, rel_err(pdf, p64).max()
     np.testing.assert_allclose(w, w64, rtol=1e-5, atol=1e-5 * np.abs(w64).max())
+    # the symmetric variant (each pair's exp once, upper-triangle tiles, FP64
+    # atomics) against the ordered one over all 2^22 rows and against FP64
+    ps, wsym = ops.empscore16(x, h, variant="symmetric")
+    ops.device_status(cuda_dev)
+    po, wo = pdf1.cpu().numpy().astype(np.float64), w1.cpu().numpy().astype(np.float64)
+    ps_np, ws_np = ps.cpu().numpy().astype(np.float64), wsym.cpu().numpy().astype(np.float64)
+    assert rel_err(ps_np, po).max() < 1e-5, rel_err(ps_np, po).max()
+    assert (np.abs(ws_np - wo) <= 1e-5 * np.abs(wo) + 1e-5 * np.abs(wo).max()).all()
+    assert rel_err(ps_np[rows], p64).max() < 1e-5
+    np.testing.assert_allclose(ws_np[rows], w64, rtol=1e-5, atol=1e-5 * np.abs(w64).max())
 
 
 def test_kde1d_2p22_by_2p20(cuda_dev):
