@@ -11,7 +11,6 @@
 
 namespace fsk {
 
-__device__ unsigned int g_device_error = 0u;
 
 static std::atomic<int64_t> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
@@ -128,13 +127,10 @@ int fsk_device_status(void* stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   cudaError_t e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return FSK_ERR_CUDA;
-  unsigned int v = 0, zero = 0;
-  e = cudaMemcpyFromSymbol(&v, g_device_error, sizeof(v));
-  if (e != cudaSuccess) return FSK_ERR_CUDA;
-  if (v != 0u) {
-    cudaMemcpyToSymbol(g_device_error, &zero, sizeof(zero));
-    return (int)(v & 0xFFu);
-  }
+  // every unit's word is read (and cleared), the first error found is returned
+  const unsigned int words[3] = {kde16_take_device_error(), score16_take_device_error(), mlp_tc_take_device_error()};
+  for (unsigned int v : words)
+    if (v != 0u) return (int)(v & 0xFFu);
   return FSK_OK;
 }
 

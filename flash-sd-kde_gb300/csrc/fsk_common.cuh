@@ -18,11 +18,25 @@
 namespace fsk {
 
 // ---- device error word ----------------------------------------------------
-// 0 = ok; otherwise an fsk_status code plus a site id in the upper bits.
-extern __device__ unsigned int g_device_error;
+// 0 = ok; otherwise an fsk_status code plus a site id in the upper bits.  Most
+// units are built without relocatable device code (no device symbol is
+// shared between units), so every translation unit has its own word; the
+// units whose kernels record errors export a take function (fsk_kernels.cuh)
+// and fsk_device_status reads and clears all of them.
+static __device__ unsigned int g_device_error = 0u;
 
 __device__ __forceinline__ void record_error(unsigned int code, unsigned int site) {
   atomicCAS(&g_device_error, 0u, code | (site << 8));
+}
+
+// This translation unit's error word, read and cleared from the host
+// (synchronous; the caller has synchronised the stream).
+static inline unsigned int take_unit_device_error() {
+  unsigned int v = 0u, zero = 0u;
+  if (cudaMemcpyFromSymbol(&v, g_device_error, sizeof(v)) != cudaSuccess) return (unsigned int)FSK_ERR_CUDA;
+  if (v != 0u && cudaMemcpyToSymbol(g_device_error, &zero, sizeof(zero)) != cudaSuccess)
+    return (unsigned int)FSK_ERR_CUDA;
+  return v;
 }
 
 // ---- host helpers -----------------------------------------------------------

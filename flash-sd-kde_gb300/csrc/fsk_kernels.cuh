@@ -4,6 +4,11 @@
 
 namespace fsk {
 
+// ---- device error words (see fsk_common.cuh) --------------------------------
+unsigned int kde16_take_device_error();    // fsk_tc_kde16.cu
+unsigned int score16_take_device_error();  // fsk_tc_score16.cu
+unsigned int mlp_tc_take_device_error();   // fsk_mlp_tc.cu
+
 // ---- fsk_api.cu -------------------------------------------------------------
 // Argument checks of fsk_kde16 (pointers, sizes, bandwidth, flags and the
 // FSK_OUT_LOG_EXACT constraints): FSK_OK or FSK_ERR_INVALID_ARGUMENT.

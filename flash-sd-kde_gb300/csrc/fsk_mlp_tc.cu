@@ -391,4 +391,7 @@ void launch_combine(const float* y, int members, int64_t batch, const float* x, 
 }
 
 }  // namespace mlp
+
+unsigned int mlp_tc_take_device_error() { return take_unit_device_error(); }
+
 }  // namespace fsk

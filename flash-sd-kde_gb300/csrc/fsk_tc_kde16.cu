@@ -707,6 +707,12 @@ __global__ void wait_timeout_probe_kernel(int* out) {
   if (threadIdx.x == 0) *out = mbar_wait(&bar, 0, 30) ? 1 : 0;
 }
 
+}  // namespace tc
+
+unsigned int kde16_take_device_error() { return take_unit_device_error(); }
+
+namespace tc {
+
 int launch_wait_timeout_probe(int* out, cudaStream_t s) {
   wait_timeout_probe_kernel<<<1, 32, 0, s>>>(out);
   count_launch();

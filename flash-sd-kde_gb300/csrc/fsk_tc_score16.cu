@@ -862,6 +862,12 @@ __global__ void __launch_bounds__(128, 1) tmem_cp_probe_kernel(const float* __re
 }
 }  // namespace
 
+}  // namespace tc
+
+unsigned int score16_take_device_error() { return take_unit_device_error(); }
+
+namespace tc {
+
 int launch_tmem_cp_probe(const float* a, uint32_t* out, cudaStream_t s) {
   tmem_cp_probe_kernel<<<1, 128, 0, s>>>(a, out);
   count_launch();

@@ -1,7 +1,9 @@
 """Builds libfsk.so in-tree from csrc/*.cu for sm_103a (GB300).
 
-Each translation unit is compiled by its own nvcc process (in parallel), then
-linked with ``nvcc -shared``.  The CUDA runtime is linked statically so the
+Each translation unit is compiled by its own nvcc process (in parallel),
+without relocatable device code except the units in RDC_UNITS (chosen by
+measurement), then linked with ``nvcc -shared`` (with the device link step
+for those units).  The CUDA runtime is linked statically so the
 library does not depend on the exact libcudart the host process has loaded.
 """
 from __future__ import annotations
@@ -23,8 +25,15 @@ ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr",
     "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
-    "-rdc=true",
 ]
+
+
+# Units compiled as relocatable device code (a device link step joins them):
+# measured on the GB300, the tensor-core KDE kernel runs 1.7 % faster built
+# this way (186.6 vs 189.8 ms at n = m = 2^20) and the score kernel 1.9 %
+# slower (410.2 vs 402.6 ms); the other units do not care.  No unit
+# references device symbols of another, so both modes link.
+RDC_UNITS = {"fsk_tc_kde16"}
 
 
 def _nvcc() -> str:
@@ -42,7 +51,7 @@ def _stale(extra_flags: list[str]) -> bool:
     if not LIB_PATH.exists():
         return True
     stamp = BUILD_DIR / "flags.txt"
-    if not stamp.exists() or stamp.read_text() != " ".join(NVCC_FLAGS + extra_flags):
+    if not stamp.exists() or stamp.read_text() != " ".join(NVCC_FLAGS + extra_flags + sorted(RDC_UNITS)):
         return True
     lib_mtime = LIB_PATH.stat().st_mtime
     deps = list(CSRC.glob("*")) + list(INCLUDE.glob("*.h"))
@@ -60,7 +69,8 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
 
     def compile_one(src: Path) -> Path:
         obj = BUILD_DIR / (src.stem + ".o")
-        cmd = [nvcc, *ARCH_FLAGS, *NVCC_FLAGS, *extra_flags, f"-I{INCLUDE}", "-c", str(src), "-o", str(obj)]
+        rdc = ["-rdc=true"] if src.stem in RDC_UNITS else []
+        cmd = [nvcc, *ARCH_FLAGS, *NVCC_FLAGS, *rdc, *extra_flags, f"-I{INCLUDE}", "-c", str(src), "-o", str(obj)]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src.name}:\n{res.stdout}\n{res.stderr}")
@@ -71,12 +81,13 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIB_PATH.with_suffix(".so.tmp")
-    cmd = [nvcc, *ARCH_FLAGS, "-rdc=true", "-shared", "-o", str(tmp), *map(str, objs)]
+    link_rdc = ["-rdc=true"] if any(o.stem in RDC_UNITS for o in objs) else []
+    cmd = [nvcc, *ARCH_FLAGS, *link_rdc, "-shared", "-o", str(tmp), *map(str, objs)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
     os.replace(tmp, LIB_PATH)
-    (BUILD_DIR / "flags.txt").write_text(" ".join(NVCC_FLAGS + extra_flags))
+    (BUILD_DIR / "flags.txt").write_text(" ".join(NVCC_FLAGS + extra_flags + sorted(RDC_UNITS)))
     return LIB_PATH
 
 
