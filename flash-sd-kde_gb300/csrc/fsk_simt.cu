@@ -223,42 +223,46 @@ int simt_score16_splits(int64_t n) {
 
 // ---------------------------------------------------------------------------
 // 16-D empirical score, symmetric (phi_ij = phi_ji: each pair's exp once).
-// Block = one row tile I (SYM_T points, thread t owns row i = I*SYM_T + t)
-// against a run of up to SYM_L column tiles J >= I.  Per column tile:
-//   phase 1 (thread = row i): phi_ij for the tile's SYM_T points from direct
-//     FP32 differences of the original coordinates; the row sums pdf_i and
-//     W_i += phi_ij (x_j - mu) accumulate in registers (per-tile partials,
-//     then compensated across the run); phi_ij goes to shared memory;
-//   phase 2 (thread = column j = J*SYM_T + t): the column sums
-//     sum_i phi_ij and sum_i phi_ij (x_i - mu) from shared memory, added to
-//     the FP64 accumulators with atomics once per tile.
-// The row sums go to the FP64 accumulators once per run.  On the diagonal
-// tile (J == I) the row side takes j >= i (self pair included) and the
-// column side j > i, so every unordered pair and the self pair count once
-// per point.
+// Block = one row tile I (SYM_R points, thread t owns row i = I*SYM_R + t)
+// against a run of up to SYM_L column tiles J of SYM_C points, J*SYM_C >=
+// I*SYM_R (upper triangle, the diagonal tiles masked).  Per column tile:
+//   phase 1 (thread = row i): phi_ij for the tile's points from direct FP32
+//     differences of the original coordinates; the row sums pdf_i and
+//     W_i += phi_ij (x_j - mu) accumulate in registers over the run; phi_ij
+//     goes to shared memory;
+//   phase 2 (thread = column j = J*SYM_C + t % SYM_C, rows t / SYM_C of the
+//     tile's two row halves): the column sums sum_i phi_ij and
+//     sum_i phi_ij (x_i - mu) from shared memory, added to the FP64
+//     accumulators with atomics once per tile.
+// The row sums go to the FP64 accumulators once per run.  Pairs with j > i
+// count on both sides; the self pair counts once (row side).
 // ---------------------------------------------------------------------------
 namespace {
-constexpr int SYM_T = 64;   // points per tile (threads per block)
+constexpr int SYM_R = 128;  // rows per block (threads)
+constexpr int SYM_C = 64;   // points per column tile
 constexpr int SYM_L = 16;   // column tiles per block
 }
 
-__global__ void __launch_bounds__(SYM_T) score16_sym_simt_kernel(
+__global__ void __launch_bounds__(SYM_R) score16_sym_simt_kernel(
     const float* __restrict__ x, int64_t n, const float* __restrict__ mu, float c2, float c2_lo,
-    int64_t n_tiles, double* __restrict__ acc_pdf, double* __restrict__ acc_w) {
+    int64_t n_col_tiles, double* __restrict__ acc_pdf, double* __restrict__ acc_w) {
   const int64_t I = blockIdx.x;
-  const int64_t J0 = I + (int64_t)blockIdx.y * SYM_L;
-  if (J0 >= n_tiles) return;   // beyond the end of this row tile's run (uniform per block)
-  const int64_t J1 = imin<int64_t>(n_tiles, J0 + SYM_L);
+  const int64_t i0 = I * SYM_R;
+  // first column tile touching the upper triangle of this row tile
+  const int64_t Jfirst = i0 / SYM_C;
+  const int64_t J0 = Jfirst + (int64_t)blockIdx.y * SYM_L;
+  if (J0 >= n_col_tiles) return;   // beyond the end of this row tile's run (uniform per block)
+  const int64_t J1 = imin<int64_t>(n_col_tiles, J0 + SYM_L);
 
-  __shared__ __align__(16) float xs[SYM_T][FSK_D];    // column tile, original coordinates
-  __shared__ __align__(16) float xcs[SYM_T][FSK_D];   // column tile, x - mu
-  __shared__ __align__(16) float xic[SYM_T][FSK_D];   // row tile, x - mu (phase 2)
-  __shared__ float phi[SYM_T][SYM_T + 1];              // [column][row], padded: conflict-free both ways
+  __shared__ __align__(16) float xs[SYM_C][FSK_D];    // column tile, original coordinates
+  __shared__ __align__(16) float xcs[SYM_C][FSK_D];   // column tile, x - mu
+  __shared__ __align__(16) float xic[SYM_R][FSK_D];   // row tile, x - mu (phase 2)
+  __shared__ float phi[SYM_C][SYM_R + 1];              // [column][row], padded: conflict-free both ways
   __shared__ float mus[FSK_D];
   const int t = threadIdx.x;
   if (t < FSK_D) mus[t] = mu[t];
   __syncthreads();
-  const int64_t i = I * SYM_T + t;
+  const int64_t i = i0 + t;
   const bool vi = i < n;
   float xi[FSK_D];
 #pragma unroll
@@ -266,93 +270,109 @@ __global__ void __launch_bounds__(SYM_T) score16_sym_simt_kernel(
     xi[k] = vi ? x[i * FSK_D + k] : 0.f;
     xic[t][k] = vi ? xi[k] - mus[k] : 0.f;
   }
-  Comp prow{0.f, 0.f};
-  Comp wrow[FSK_D];
+  float prow = 0.f, wrow[FSK_D];
 #pragma unroll
-  for (int k = 0; k < FSK_D; ++k) wrow[k] = Comp{0.f, 0.f};
+  for (int k = 0; k < FSK_D; ++k) wrow[k] = 0.f;
+  const int cj = t % SYM_C, rh = t / SYM_C;   // phase 2: column and row half
 
   for (int64_t J = J0; J < J1; ++J) {
-    const int64_t j0 = J * SYM_T;
-    const int validj = (int)imin<int64_t>(SYM_T, n - j0);
-    const bool diag = J == I;
+    const int64_t j0 = J * SYM_C;
+    const int validj = (int)imin<int64_t>(SYM_C, n - j0);
     __syncthreads();   // previous tile's phase 2 is done with phi / xs
-    for (int e = t; e < SYM_T * FSK_D; e += SYM_T) {
+    for (int e = t; e < SYM_C * FSK_D; e += SYM_R) {
       const int r = e / FSK_D, k = e % FSK_D;
       const float v = r < validj ? x[(j0 + r) * FSK_D + k] : 0.f;
       xs[r][k] = v;
       xcs[r][k] = r < validj ? v - mus[k] : 0.f;
     }
     __syncthreads();
-    // phase 1: row i against the tile's points
+    // phase 1: row i against the tile's points (j <= i drops from the column
+    // side, j < i from both: those pairs belong to an earlier row tile's run)
     float ps = 0.f, wp[FSK_D];
 #pragma unroll
     for (int k = 0; k < FSK_D; ++k) wp[k] = 0.f;
-    for (int r = 0; r < SYM_T; ++r) {
-      float xv[FSK_D], xc[FSK_D];
+    const int64_t dj = i - j0;   // column index of the diagonal in this tile (may be outside)
+    for (int r = 0; r < SYM_C; ++r) {
+      const float4* xr = reinterpret_cast<const float4*>(&xs[r][0]);
+      float d0 = 0.f, d1 = 0.f, d2 = 0.f, d3 = 0.f;
 #pragma unroll
-      for (int k = 0; k < FSK_D; k += 4) {
-        const float4 v = *reinterpret_cast<const float4*>(&xs[r][k]);
-        xv[k] = v.x; xv[k + 1] = v.y; xv[k + 2] = v.z; xv[k + 3] = v.w;
-        const float4 c = *reinterpret_cast<const float4*>(&xcs[r][k]);
-        xc[k] = c.x; xc[k + 1] = c.y; xc[k + 2] = c.z; xc[k + 3] = c.w;
+      for (int kk = 0; kk < 4; ++kk) {
+        const float4 v = xr[kk];
+        const float a0 = xi[4 * kk] - v.x, a1 = xi[4 * kk + 1] - v.y;
+        const float a2 = xi[4 * kk + 2] - v.z, a3 = xi[4 * kk + 3] - v.w;
+        d0 = fmaf(a0, a0, d0);
+        d1 = fmaf(a1, a1, d1);
+        d2 = fmaf(a2, a2, d2);
+        d3 = fmaf(a3, a3, d3);
       }
-      const bool ok = vi && r < validj;
-      const float e = ok ? exp2_neg_scaled(sqdist16(xi, xv), c2, c2_lo) : 0.f;
-      const float er = (!diag || r >= t) ? e : 0.f;
-      ps += er;
+      const bool ok = vi && r < validj && r >= dj;   // j >= i
+      const float e = ok ? exp2_neg_scaled((d0 + d1) + (d2 + d3), c2, c2_lo) : 0.f;
+      ps += e;
+      const float4* xcr = reinterpret_cast<const float4*>(&xcs[r][0]);
 #pragma unroll
-      for (int k = 0; k < FSK_D; ++k) wp[k] = fmaf(er, xc[k], wp[k]);
-      phi[r][t] = (!diag || r > t) ? e : 0.f;
+      for (int kk = 0; kk < 4; ++kk) {
+        const float4 c = xcr[kk];
+        wp[4 * kk] = fmaf(e, c.x, wp[4 * kk]);
+        wp[4 * kk + 1] = fmaf(e, c.y, wp[4 * kk + 1]);
+        wp[4 * kk + 2] = fmaf(e, c.z, wp[4 * kk + 2]);
+        wp[4 * kk + 3] = fmaf(e, c.w, wp[4 * kk + 3]);
+      }
+      phi[r][t] = r > dj ? e : 0.f;   // column side: j > i only
     }
-    prow.add(ps);
+    prow += ps;
 #pragma unroll
-    for (int k = 0; k < FSK_D; ++k) wrow[k].add(wp[k]);
+    for (int k = 0; k < FSK_D; ++k) wrow[k] += wp[k];
     __syncthreads();
-    // phase 2: column j = j0 + t against the row tile
-    if (t < validj) {
+    // phase 2: column j = j0 + cj against rows rh * SYM_C .. +SYM_C of the tile
+    if (cj < validj) {
       float pc = 0.f, wc[FSK_D];
 #pragma unroll
       for (int k = 0; k < FSK_D; ++k) wc[k] = 0.f;
-      for (int r = 0; r < SYM_T; ++r) {
-        const float e = phi[t][r];
+      const int rbeg = rh * SYM_C;
+      for (int r = rbeg; r < rbeg + SYM_C; ++r) {
+        const float e = phi[cj][r];
+        const float4* c4 = reinterpret_cast<const float4*>(&xic[r][0]);
 #pragma unroll
-        for (int k = 0; k < FSK_D; k += 4) {
-          const float4 c = *reinterpret_cast<const float4*>(&xic[r][k]);
-          wc[k] = fmaf(e, c.x, wc[k]);
-          wc[k + 1] = fmaf(e, c.y, wc[k + 1]);
-          wc[k + 2] = fmaf(e, c.z, wc[k + 2]);
-          wc[k + 3] = fmaf(e, c.w, wc[k + 3]);
+        for (int kk = 0; kk < 4; ++kk) {
+          const float4 c = c4[kk];
+          wc[4 * kk] = fmaf(e, c.x, wc[4 * kk]);
+          wc[4 * kk + 1] = fmaf(e, c.y, wc[4 * kk + 1]);
+          wc[4 * kk + 2] = fmaf(e, c.z, wc[4 * kk + 2]);
+          wc[4 * kk + 3] = fmaf(e, c.w, wc[4 * kk + 3]);
         }
         pc += e;
       }
-      const int64_t j = j0 + t;
-      atomicAdd(&acc_pdf[j], (double)pc);
+      if (pc != 0.f) {
+        const int64_t j = j0 + cj;
+        atomicAdd(&acc_pdf[j], (double)pc);
 #pragma unroll
-      for (int k = 0; k < FSK_D; ++k) atomicAdd(&acc_w[j * FSK_D + k], (double)wc[k]);
+        for (int k = 0; k < FSK_D; ++k) atomicAdd(&acc_w[j * FSK_D + k], (double)wc[k]);
+      }
     }
   }
   if (vi) {
-    atomicAdd(&acc_pdf[i], (double)prow.s + (double)prow.c);
+    atomicAdd(&acc_pdf[i], (double)prow);
 #pragma unroll
-    for (int k = 0; k < FSK_D; ++k) atomicAdd(&acc_w[i * FSK_D + k], (double)wrow[k].s + (double)wrow[k].c);
+    for (int k = 0; k < FSK_D; ++k) atomicAdd(&acc_w[i * FSK_D + k], (double)wrow[k]);
   }
 }
 
 void launch_score16_sym_simt(const float* x, int64_t n, const float* mu, double h, double* acc_pdf,
                              double* acc_w, cudaStream_t s) {
-  const int64_t n_tiles = (n + SYM_T - 1) / SYM_T;
+  const int64_t row_tiles = (n + SYM_R - 1) / SYM_R;
+  const int64_t col_tiles = (n + SYM_C - 1) / SYM_C;
   const double c2d = FSK_LOG2E / (2.0 * h * h);
   const float c2 = (float)c2d, c2_lo = (float)(c2d - (double)c2);
-  // grid.x: row tile; grid.y: run index (runs past the last tile exit at once)
-  const dim3 grid((unsigned)n_tiles, (unsigned)((n_tiles + SYM_L - 1) / SYM_L));
+  // grid.x: row tile; grid.y: run index (runs past the last column tile exit at once)
+  const dim3 grid((unsigned)row_tiles, (unsigned)((col_tiles + SYM_L - 1) / SYM_L));
   TimerScope ts(K_SCORE16_SYM_SIMT, 0.5 * (double)n * (double)(n + 1), s);
-  score16_sym_simt_kernel<<<grid, SYM_T, 0, s>>>(x, n, mu, c2, c2_lo, n_tiles, acc_pdf, acc_w);
+  score16_sym_simt_kernel<<<grid, SYM_R, 0, s>>>(x, n, mu, c2, c2_lo, col_tiles, acc_pdf, acc_w);
   count_launch();
 }
 
 int64_t sym_simt_pairs(int64_t n) {
-  const int64_t n_tiles = (n + SYM_T - 1) / SYM_T;
-  return n_tiles * (n_tiles + 1) / 2;
+  const int64_t col_tiles = (n + SYM_C - 1) / SYM_C;
+  return col_tiles * (col_tiles + 1) / 2;
 }
 
 // ---------------------------------------------------------------------------
