@@ -58,7 +58,7 @@ namespace tc {
 namespace {
 
 constexpr int SNQT = 2;                                    // query tiles per unit (256 queries)
-constexpr int SNS = 5;                                     // data stages
+constexpr int SNS = 4;                                     // data stages
 constexpr int XT_ROW_BYTES = NT * 2;                       // one feature row over 64 points, fp16
 constexpr int XT_BYTES = FSK_D * XT_ROW_BYTES;             // 2 KB
 constexpr int S_XTH_OFFSET = B_L_OFFSET + B_L_BYTES;       // 8 KB
@@ -73,7 +73,7 @@ constexpr int S_MMA_WARP2 = S_EPI_WARPS + 2;    // issues the S MMAs of query ti
 constexpr int W_MMA_WARP = S_EPI_WARPS + 3;     // first of the W_ISSUERS weighted-sum issuers
 constexpr int W_ISSUERS = 2 * SNQT;             // (query tile, weight part hi / lo)
 constexpr int S_THREADS = (S_EPI_WARPS + 3 + W_ISSUERS) * 32;
-constexpr int S_GROUP = 16;                                // data tiles per W accumulation
+constexpr int S_GROUP = 32;                                // data tiles per W accumulation
 constexpr int NBUF = 2;                                    // S / weight buffers in TMEM
 constexpr int WN = 2 * FSK_D;                              // W MMA N, hi weights: X_hi and X_lo rows
 constexpr int WN_LO = FSK_D;                               // W MMA N, lo weights: X_hi rows
