@@ -73,7 +73,7 @@ constexpr int S_MMA_WARP2 = S_EPI_WARPS + 2;    // issues the S MMAs of query ti
 constexpr int W_MMA_WARP = S_EPI_WARPS + 3;     // first of the W_ISSUERS weighted-sum issuers
 constexpr int W_ISSUERS = 2 * SNQT;             // (query tile, weight part hi / lo)
 constexpr int S_THREADS = (S_EPI_WARPS + 3 + W_ISSUERS) * 32;
-constexpr int S_GROUP = 32;                                // data tiles per W accumulation
+constexpr int S_GROUP = 16;                                // data tiles per W accumulation
 constexpr int NBUF = 2;                                    // S / weight buffers in TMEM
 constexpr int WN = 2 * FSK_D;                              // W MMA N, hi weights: X_hi and X_lo rows
 constexpr int WN_LO = FSK_D;                               // W MMA N, lo weights: X_hi rows
