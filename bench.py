@@ -58,7 +58,8 @@ C_OPS_PER_PAIR = 3.0
 K_OPS_PER_POLY_EXP = 10.0
 KERNEL_NAMES = {1: "kde16_tc_kernel", 2: "kde16_simt_kernel", 3: "score16_simt_kernel",
                 4: "score16_sym_simt_kernel", 5: "kde1d_kernel", 6: "kde1d_score_kernel",
-                7: "score16_tc_kernel", 8: "score16_sym_tc_kernel"}
+                7: "score16_tc_kernel", 9: "mlp_infer_kernel", 10: "kde16_logspace_kernel",
+                11: "kde_nd_kernel", 12: "score_nd_kernel"}
 # Tensor-core flops per pair evaluation.  "issued": what the tcgen05 kernels
 # execute (three-part fp16 operands: seven K=16 MMAs for the exponent; the
 # score kernel's weighted sums as fp16 hi/lo weights times [X_hi | X_lo] and
@@ -67,6 +68,23 @@ KERNEL_NAMES = {1: "kde16_tc_kernel", 2: "kde16_simt_kernel", 3: "score16_simt_k
 MMA_FLOPS_PER_PAIR = {"kde16_tc_kernel": {"issued": 7 * 2 * 16, "algorithmic": 2 * 16},
                       "score16_tc_kernel": {"issued": 7 * 2 * 16 + 2 * 128 * 16 * (4 * 32 + 4 * 16) / (128 * 64),
                                             "algorithmic": 2 * 2 * 16}}
+
+
+def log_density_errors(dens, ref_logp) -> dict:
+    """Errors of densities against FP64 log-densities: the density's relative
+    error, the absolute log-density error and the relative log-density error
+    |log p - log p64| / |log p64| (the error measure of the 1e-5 target)."""
+    import numpy as np
+
+    dens = np.asarray(dens, dtype=np.float64)
+    ref = np.asarray(ref_logp, dtype=np.float64)
+    rel = np.abs(dens - np.exp(ref)) / np.exp(ref)
+    logp = np.log(np.maximum(dens, np.finfo(np.float64).tiny))
+    abs_log = np.abs(logp - ref)
+    return {"kde_max_rel_vs_fp64": float(rel.max()), "kde_median_rel_vs_fp64": float(np.median(rel)),
+            "kde_max_abs_log_err_vs_fp64": float(abs_log.max()),
+            "kde_max_rel_log_err_vs_fp64": float((abs_log / np.abs(ref)).max()),
+            "kde_queries_checked": int(dens.size)}
 
 
 def parse():
@@ -285,9 +303,7 @@ def run_triton_leg(args) -> None:
 
     def errors(deb, kde_of_x):
         dens = kde_of_x.detach().cpu().numpy().astype(np.float64)
-        rel = np.abs(dens - np.exp(ref_logp)) / np.exp(ref_logp)
-        return {"kde_max_rel_vs_fp64": float(rel.max()), "kde_median_rel_vs_fp64": float(np.median(rel)),
-                "kde_queries_checked": sub_q,
+        return {**log_density_errors(dens, ref_logp),
                 "debias_max_abs_vs_fp64": float(np.abs(deb[:64].detach().cpu().numpy() - deb64).max()),
                 "debias_rows_checked": 64}
 
@@ -541,7 +557,7 @@ def run_gpu_arm(args) -> None:
     deb_np = deb.cpu().numpy()
     dens_np = dens.cpu().numpy().astype(np.float64)
     ref_logp = fp64.log_density(deb_np, q_np[sub], h)
-    kde_rel = np.abs(dens_np[sub] - np.exp(ref_logp)) / np.exp(ref_logp)
+    kde_err = log_density_errors(dens_np[sub], ref_logp)
     pdf64, w64 = fp64.empirical_score_rows(x_np, np.arange(64), h)
     deb64 = x_np[:64].astype(np.float64) + 0.5 * (w64 / (pdf64[:, None] + EPS) - x_np[:64])
     deb_abs = float(np.abs(deb_np[:64] - deb64).max())
@@ -602,8 +618,7 @@ def run_gpu_arm(args) -> None:
             "cpu_baseline": cpu,
             "surrogate": surrogate,
             "clocks": sampler.summary(),
-            "accuracy": {"kde_max_rel_vs_fp64": float(kde_rel.max()), "kde_queries_checked": int(kde_rel.size),
-                         "debias_max_abs_vs_fp64": deb_abs, "debias_rows_checked": 64},
+            "accuracy": {**kde_err, "debias_max_abs_vs_fp64": deb_abs, "debias_rows_checked": 64},
             "step_ms": step_ms,
         }
         print(json.dumps(line), flush=True)
