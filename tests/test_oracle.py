@@ -95,3 +95,22 @@ def test_log_error_metrics():
     assert abs(m["max_abs_log_err"] - 2e-6) < 1e-12
     assert abs(m["mean_abs_log_err"] - 1e-6) < 1e-12
     assert abs(m["bias_log_err"] - (-1e-6 / 3)) < 1e-12
+
+
+def test_timed_cpu_baseline_tiles_match_oracle():
+    """The timed CPU baseline's tiled blocks compute the oracle's sums (FP32
+    tolerance: only the grouping of the sums differs)."""
+    from oracle import cpu_baseline as C
+
+    rng = np.random.default_rng(5)
+    n = 3 * C.COL_BLOCK + 77          # ragged last column tile
+    x = rng.standard_normal((n, 16)).astype(np.float32)
+    q = (rng.standard_normal((40, 16)) * 0.8).astype(np.float32)
+    h = 0.9
+    xn = (x * x).sum(axis=1)
+    pdf, w = C._score_block(x, xn, 10, 50, h)
+    pdf_ref, w_ref, _ = R.empirical_score_nd_numpy(x, h)
+    np.testing.assert_allclose(pdf, pdf_ref[10:50], rtol=2e-5)
+    np.testing.assert_allclose(w, w_ref[10:50], rtol=2e-4, atol=2e-4 * np.abs(w_ref[10:50]).max())
+    norm = 1.0 / ((2.0 * np.pi) ** 8 * h ** 16 * n)
+    np.testing.assert_allclose(norm * C._kde_block(x, xn, q, h), R.kde_eval_nd_numpy(q, x, h), rtol=2e-5)
