@@ -15,8 +15,8 @@ reference; it serves bulk queries of a fitted Flash-SD-KDE model).
   gate: a query is served by the surrogate when the members agree
   (max - min <= spread_tol, in log units) and its whitened radius is inside
   the training distribution (r^2 <= the radius_quantile of the training
-  queries); every other query falls back to the exact KDE kernel, so the
-  exact path is also the judge of the surrogate's error.
+  queries); every other query falls back to the exact KDE kernel, which is
+  also what measures the surrogate's error.
 """
 from __future__ import annotations
 
