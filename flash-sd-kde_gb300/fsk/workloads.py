@@ -12,6 +12,9 @@ student_t_16d    multivariate Student-t (nu = 5), per-axis scale 10^U(-1, 1),
 lowrank_16d      z diag(k^-1/2), k = 1..16, z ~ N(0, I).
 gmm3_1d          1-D mixture: means (-2, 0, 3), std (0.5, 1, 0.3),
                  weights (0.3, 0.5, 0.2); grid queries on [-5, 6].
+gm_diag_16d      the error-suite smoke configuration: 4-component diagonal
+                 mixture, means N(0, I) * 2, unit per-axis std, equal weights,
+                 8192 train / 4096 test, standardised by the train statistics.
 """
 from __future__ import annotations
 
@@ -87,6 +90,31 @@ def gmm3_1d(n: int, seed: int = 0) -> np.ndarray:
 
 def grid_1d(m: int, lo: float = -5.0, hi: float = 6.0) -> np.ndarray:
     return np.linspace(lo, hi, m).astype(np.float32)
+
+
+def gm_diag_16d(n_train: int = 8192, n_test: int = 4096, seed: int = 0, n_components: int = 4,
+                component_std: float = 1.0, mean_scale: float = 2.0):
+    """Train and test points of the reference's error-suite smoke run
+    (configs/error_suite_16d/smoke.yaml; recipe of
+    experiments/error_suite_16d/datasets.py:34-42 and :55-78, sampling of
+    truth.py:57-63): component means ~ N(0, I) * mean_scale drawn with `seed`,
+    equal weights, per-axis std `component_std`; the train set is sampled
+    with `seed` and the test set with `seed + 1` (component index, then the
+    Gaussian offsets); both are standardised by the train mean and unbiased
+    per-axis std.  Returns float32 (train, test)."""
+    rng = np.random.default_rng(seed)
+    means = rng.normal(size=(n_components, D)) * mean_scale
+    weights = np.full(n_components, 1.0 / n_components)
+
+    def draw(count: int, s: int) -> np.ndarray:
+        g = np.random.default_rng(s)
+        comp = g.choice(n_components, size=count, p=weights)
+        return g.normal(size=(count, D)) * component_std + means[comp]
+
+    train, test = draw(n_train, seed), draw(n_test, seed + 1)
+    mu, sd = train.mean(axis=0), train.std(axis=0, ddof=1)
+    sd = np.where(sd <= 0, 1.0, sd)
+    return ((train - mu) / sd).astype(np.float32), ((test - mu) / sd).astype(np.float32)
 
 
 def shard(count: int, world: int, rank: int) -> tuple[int, int]:

@@ -275,6 +275,28 @@ def test_kde_eval_log_eps0_and_estimator_log_space(cuda_dev):
 
 
 
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_error_suite_smoke_configuration(cuda_dev, precision):
+    """The reference's error-suite smoke run (experiments/error_suite_16d,
+    configs/error_suite_16d/smoke.yaml: 4-component diagonal mixture, 8192
+    train / 4096 test, standardised, Silverman-diag bandwidth, log-density
+    output against the FP64 log-space reference): every log-density finite,
+    max / p95 / mean absolute log error against FP64 within 1e-5 / 2e-6 / 1e-6
+    (the reference's test asks for a finite maximum)."""
+    from flash_sd_kde.kde import kde_eval_log
+    from fsk import workloads
+
+    train, test = workloads.gm_diag_16d()
+    h = fp64.silverman_nd(train)
+    ref = fp64.log_density(train, test, h)
+    mode = "fast_tf32" if precision == "tensor" else "fp32_ieee"
+    out = kde_eval_log(torch.from_numpy(train).to(cuda_dev), torch.from_numpy(test).to(cuda_dev), h, eps=0.0,
+                       device=cuda_dev, precision_mode=mode).cpu().numpy()
+    m = fp64.log_error_metrics(out, ref)
+    assert m["finite_fraction"] == 1.0
+    assert m["max_abs_log_err"] < 1e-5 and m["p95_abs_log_err"] < 2e-6 and m["mean_abs_log_err"] < 1e-6, m
+
+
 @pytest.mark.parametrize("name", ["kde16_plain_4096x1024", "kde16_seed1", "kde16_seed11"])
 def test_exp_offload_vs_reference_and_fp64(cuda_dev, golden, name):
     """FSK_EXP_OFFLOAD: a quarter of the exps by the FMA-pipe polynomial

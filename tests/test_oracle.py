@@ -114,3 +114,20 @@ def test_timed_cpu_baseline_tiles_match_oracle():
     np.testing.assert_allclose(w, w_ref[10:50], rtol=2e-4, atol=2e-4 * np.abs(w_ref[10:50]).max())
     norm = 1.0 / ((2.0 * np.pi) ** 8 * h ** 16 * n)
     np.testing.assert_allclose(norm * C._kde_block(x, xn, q, h), R.kde_eval_nd_numpy(q, x, h), rtol=2e-5)
+
+
+def test_error_suite_smoke_configuration_oracle():
+    """The reference's error-suite smoke run on the CPU (its fallback without
+    CUDA): the FP64 log-space oracle gives finite log-densities for every test
+    query of the 4-component diagonal mixture."""
+    from fsk import workloads
+
+    train, test = workloads.gm_diag_16d()
+    assert train.shape == (8192, 16) and test.shape == (4096, 16)
+    np.testing.assert_allclose(train.mean(axis=0), 0.0, atol=1e-5)
+    np.testing.assert_allclose(train.std(axis=0, ddof=1), 1.0, rtol=1e-5)
+    h = fp64.silverman_nd(train)
+    ref = fp64.log_density(train, test, h)
+    m = fp64.log_error_metrics(ref, ref)
+    assert m["finite_fraction"] == 1.0 and m["max_abs_log_err"] == 0.0
+    assert np.all(ref < 0) and np.all(ref > -200)
