@@ -173,6 +173,52 @@ def test_surrogate_gate_and_exact_fallback(cuda_dev):
     assert bool((spread[served] <= sur.spread_tol).all())
 
 
+def test_surrogate_checkpoint_and_resume(cuda_dev, tmp_path):
+    """save / load / resume: a loaded surrogate serves bit-identical values;
+    resuming continues the step count and the AdamW state on the same
+    (regenerated) training pairs, from the original and from the loaded copy
+    alike; a surrogate fitted on given queries refuses to resume without
+    them."""
+    from flash_sd_kde.surrogate import SurrogateKDE
+    from fsk import ops, workloads
+
+    x_np, _ = workloads.gmm8_16d(4096, 16)
+    x = torch.from_numpy(x_np).to(cuda_dev)
+    h = float(ops.silverman(x).item())
+    sur = SurrogateKDE(members=2, epochs=2, batch_size=4096, spread_tol=0.5, seed=4).fit(x, h, n_pairs=65536)
+    steps = sur.step_
+    assert steps == 2 * (65536 // 4096) and sur.total_steps_ == steps
+    path = tmp_path / "sur.pt"
+    sur.save(path)
+    back = SurrogateKDE.load(path, device=cuda_dev)
+    g = torch.Generator(device=cuda_dev).manual_seed(11)
+    q = (x[torch.randint(4096, (5000,), generator=g, device=cuda_dev)]
+         + torch.randn((5000, 16), generator=g, device=cuda_dev) * h).contiguous()
+    for a, b in zip(sur.predict(q), back.predict(q)):
+        assert torch.equal(a, b)
+    assert torch.equal(sur.score_samples(q), back.score_samples(q))
+    assert torch.equal(back.adam_m_, sur.adam_m_) and torch.equal(back.adam_v_, sur.adam_v_)
+    assert back.history == sur.history and back.r2_max_ == sur.r2_max_
+    sur.resume(2)
+    back.resume(2)
+    ops.device_status(cuda_dev)
+    assert sur.step_ == back.step_ == 2 * steps and len(sur.history) == len(back.history) == 4
+    # the same pairs in the same order from the same state: equal up to the order of the
+    # weight-gradient atomics
+    np.testing.assert_allclose(back.history, sur.history, rtol=2e-2)
+    assert sur.history[3] < sur.history[0]
+    assert not torch.equal(back.params_, SurrogateKDE.load(path, device=cuda_dev).params_)
+    given = SurrogateKDE(members=2, epochs=1, batch_size=4096, seed=4).fit(x, h, queries=q,
+                                                                          log_density=sur._exact_logp(q))
+    with pytest.raises(ValueError):
+        given.resume(1)
+    given.resume(1, queries=q, log_density=sur._exact_logp(q))
+    assert given.step_ == 2 * (5000 // 4096)
+    with pytest.raises(ValueError):
+        torch.save({"format": "other"}, tmp_path / "bad.pt")
+        SurrogateKDE.load(tmp_path / "bad.pt", device=cuda_dev)
+
+
 def test_surrogate_gain_over_exact_only(cuda_dev):
     """What the trained network gains over the method without it, on the
     learned-surrogate configuration (exact SD-KDE of 262144 8-component
