@@ -142,6 +142,7 @@ size_t fsk_kde16_workspace_bytes(int64_t m, int64_t n, int flags) {
 int fsk_kde16(const float* queries, int64_t m, const float* data, int64_t n, double bandwidth, int flags,
               double out_scale, double out_eps, float* out, void* workspace, size_t workspace_bytes,
               void* stream) {
+  NvtxRange nvtx_range("fsk_kde16");
   int st = validate_kde16_args(queries, m, data, n, bandwidth, flags, out_eps, out);
   if (st) return st;
   st = check_device();
@@ -211,6 +212,7 @@ size_t fsk_empscore16_workspace_bytes(int64_t n, int variant, int flags) {
 
 int fsk_empscore16(const float* data, int64_t n, double bandwidth, int variant, int flags, float* pdf_sum,
                    float* weighted_sum, void* workspace, size_t workspace_bytes, void* stream) {
+  NvtxRange nvtx_range("fsk_empscore16");
   if (!data || !pdf_sum || !weighted_sum || n < 1 || bad_bw(bandwidth)) return FSK_ERR_INVALID_ARGUMENT;
   if (variant != FSK_SCORE_ORDERED && variant != FSK_SCORE_SYMMETRIC) return FSK_ERR_INVALID_ARGUMENT;
   if (flags & ~(KNOWN_FLAGS & ~(FSK_PREC_FP16_SINGLE | FSK_EXP_OFFLOAD))) return FSK_ERR_INVALID_ARGUMENT;
@@ -252,6 +254,7 @@ int fsk_empscore16(const float* data, int64_t n, double bandwidth, int variant, 
 int fsk_debias16(const float* data, int64_t n, const float* pdf_sum, const float* weighted_sum,
                  int64_t w_row_stride, int64_t w_col_stride, double bandwidth, double eps, float* debiased,
                  float* score, void* stream) {
+  NvtxRange nvtx_range("fsk_debias16");
   if (!data || !pdf_sum || !weighted_sum || !debiased || n < 1 || bad_bw(bandwidth) || !(eps >= 0.0))
     return FSK_ERR_INVALID_ARGUMENT;
   int st = check_device();
@@ -287,6 +290,7 @@ size_t fsk_sdkde16_workspace_bytes(int64_t n, int64_t m, int flags) {
 int fsk_sdkde16(const float* data, int64_t n, const float* queries, int64_t m, double bandwidth, int flags,
                 double eps, double out_scale, double out_eps, float* debiased, float* out, void* workspace,
                 size_t workspace_bytes, void* stream) {
+  NvtxRange nvtx_range("fsk_sdkde16");
   if (!data || !queries || !out || n < 1 || m < 1 || bad_bw(bandwidth) || !(eps >= 0.0))
     return FSK_ERR_INVALID_ARGUMENT;
   if (flags & ~kSdkdeKdeFlags) return FSK_ERR_INVALID_ARGUMENT;
@@ -321,6 +325,7 @@ size_t fsk_kde_nd_workspace_bytes(int64_t m, int64_t n, int d, int flags) {
 
 int fsk_kde_nd(const float* queries, int64_t m, const float* data, int64_t n, int d, double bandwidth, int flags,
                double out_scale, double out_eps, float* out, void* workspace, size_t workspace_bytes, void* stream) {
+  NvtxRange nvtx_range("fsk_kde_nd");
   if (!queries || !data || !out || m < 1 || n < 1 || d < 1 || d > FSK_ND_MAX || bad_bw(bandwidth))
     return FSK_ERR_INVALID_ARGUMENT;
   if (flags & ~(FSK_PREC_IEEE | FSK_LAPLACE | FSK_OUT_LOG | FSK_ATOMIC)) return FSK_ERR_INVALID_ARGUMENT;
@@ -352,6 +357,7 @@ size_t fsk_empscore_nd_workspace_bytes(int64_t n, int d) {
 
 int fsk_empscore_nd(const float* data, int64_t n, int d, double bandwidth, float* pdf_sum, float* weighted_sum,
                     void* workspace, size_t workspace_bytes, void* stream) {
+  NvtxRange nvtx_range("fsk_empscore_nd");
   if (!data || !pdf_sum || !weighted_sum || n < 1 || d < 1 || d > FSK_ND_MAX || bad_bw(bandwidth))
     return FSK_ERR_INVALID_ARGUMENT;
   int st = check_device();
@@ -370,6 +376,7 @@ int fsk_empscore_nd(const float* data, int64_t n, int d, double bandwidth, float
 
 int fsk_debias_nd(const float* data, int64_t n, int d, const float* pdf_sum, const float* weighted_sum,
                   double bandwidth, double eps, float* debiased, float* score, void* stream) {
+  NvtxRange nvtx_range("fsk_debias_nd");
   if (!data || !pdf_sum || !weighted_sum || !debiased || n < 1 || d < 1 || d > FSK_ND_MAX || bad_bw(bandwidth) ||
       !(eps >= 0.0))
     return FSK_ERR_INVALID_ARGUMENT;
@@ -391,6 +398,7 @@ size_t fsk_kde1d_workspace_bytes(int64_t m, int64_t n, int flags) {
 int fsk_kde1d(const float* queries, int64_t m, const float* data, int64_t n, double bandwidth, int flags,
               double out_scale, double out_eps, float* out, void* workspace, size_t workspace_bytes,
               void* stream) {
+  NvtxRange nvtx_range("fsk_kde1d");
   if (!queries || !data || !out || m < 1 || n < 1 || bad_bw(bandwidth)) return FSK_ERR_INVALID_ARGUMENT;
   if (flags & ~KNOWN_FLAGS) return FSK_ERR_INVALID_ARGUMENT;
   int st = check_device();
@@ -410,6 +418,7 @@ int fsk_kde1d(const float* queries, int64_t m, const float* data, int64_t n, dou
 int fsk_kde1d_score(const float* queries, int64_t m, const float* data, int64_t n, double bandwidth,
                     float* score, float* pdf, float* deriv, void* workspace, size_t workspace_bytes,
                     void* stream) {
+  NvtxRange nvtx_range("fsk_kde1d_score");
   if (!queries || !data || m < 1 || n < 1 || bad_bw(bandwidth)) return FSK_ERR_INVALID_ARGUMENT;
   int st = check_device();
   if (st) return st;
@@ -431,6 +440,7 @@ size_t fsk_silverman_workspace_bytes(int64_t n, int d) {
 
 int fsk_silverman(const float* data, int64_t n, int d, int rule, double* h_out, void* workspace,
                   size_t workspace_bytes, void* stream) {
+  NvtxRange nvtx_range("fsk_silverman");
   if (!data || !h_out || n < 1 || d < 1 || d > 64) return FSK_ERR_INVALID_ARGUMENT;
   if (rule != FSK_RULE_SILVERMAN && rule != FSK_RULE_SDKDE_1D) return FSK_ERR_INVALID_ARGUMENT;
   if (rule == FSK_RULE_SDKDE_1D && d != 1) return FSK_ERR_INVALID_ARGUMENT;
@@ -441,6 +451,7 @@ int fsk_silverman(const float* data, int64_t n, int d, int rule, double* h_out, 
 }
 
 int fsk_reduce_partials(const float* partials, int64_t splits, int64_t count, float* out, void* stream) {
+  NvtxRange nvtx_range("fsk_reduce_partials");
   if (!partials || !out || splits < 1 || count < 0) return FSK_ERR_INVALID_ARGUMENT;
   if (count == 0) return FSK_OK;
   int st = check_device();

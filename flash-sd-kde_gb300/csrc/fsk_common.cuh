@@ -7,6 +7,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 #include <string.h>
 
@@ -58,6 +59,17 @@ enum KernelId {
   K_KDE16_LOGSPACE = 10,   // shifted recompute of underflowing queries (work not known on the host)
   K_KDE_ND = 11,
   K_SCORE_ND = 12,
+};
+
+// Host-side NVTX range around one C-ABI entry point, so profilers (ncu
+// --nvtx, Nsight Systems) show each phase (score, debias, KDE, ...) by name;
+// NVTX v3 is header-only and its calls do nothing unless a tool is attached.
+class NvtxRange {
+ public:
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
 };
 
 // RAII bracket of one kernel launch with CUDA events on its stream when the

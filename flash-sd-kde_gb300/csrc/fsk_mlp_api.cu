@@ -84,6 +84,7 @@ int fsk_mlp_pack(const float* params, int members, const float* in_mean, const f
 }
 
 int fsk_mlp_infer(const void* packed, int members, const float* x, int64_t batch, float* y, void* stream) {
+  NvtxRange nvtx_range("fsk_mlp_infer");
   if (!packed || !x || !y || bad_members(members) || batch < 1 || (reinterpret_cast<uintptr_t>(x) & 15) ||
       (reinterpret_cast<uintptr_t>(packed) & 15))
     return FSK_ERR_INVALID_ARGUMENT;
@@ -95,6 +96,7 @@ int fsk_mlp_infer(const void* packed, int members, const float* x, int64_t batch
 int fsk_mlp_combine(const float* y, int members, int64_t batch, const float* x, const float* in_mean,
                     const float* in_inv_std, float base_a, float base_b, float spread_tol, float r2_max, float* mean,
                     float* spread, uint8_t* served, void* stream) {
+  NvtxRange nvtx_range("fsk_mlp_combine");
   if (!y || bad_members(members) || batch < 1 || (x && (!in_mean || !in_inv_std))) return FSK_ERR_INVALID_ARGUMENT;
   int st = check_device();
   if (st) return st;
