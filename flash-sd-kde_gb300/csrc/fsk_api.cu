@@ -119,6 +119,7 @@ const char* fsk_strerror(int status) {
     case FSK_ERR_DEVICE_TIMEOUT: return "bounded device wait timed out";
     case FSK_ERR_UNSUPPORTED_DEVICE: return "device is not sm_103 (GB300)";
     case FSK_ERR_SCRATCH_LIMIT: return "request exceeds the fixed scratch limit";
+    case FSK_ERR_DEVICE_BOUNDS: return "device index out of bounds (bounds-check build)";
     default: return "unknown status";
   }
 }
@@ -131,6 +132,12 @@ int fsk_device_status(void* stream) {
   const unsigned int words[3] = {kde16_take_device_error(), score16_take_device_error(), mlp_tc_take_device_error()};
   for (unsigned int v : words)
     if (v != 0u) return (int)(v & 0xFFu);
+#ifdef FSK_BOUNDS_CHECK
+  // units whose only device errors are the bounds checks
+  const unsigned int checked[3] = {simt_take_device_error(), reduce_take_device_error(), logspace_take_device_error()};
+  for (unsigned int v : checked)
+    if (v != 0u) return (int)(v & 0xFFu);
+#endif
   return FSK_OK;
 }
 

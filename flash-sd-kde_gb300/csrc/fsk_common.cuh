@@ -30,6 +30,24 @@ __device__ __forceinline__ void record_error(unsigned int code, unsigned int sit
   atomicCAS(&g_device_error, 0u, code | (site << 8));
 }
 
+// Bounds-check build (-DFSK_BOUNDS_CHECK; fsk._build.build(checked=True)
+// makes libfsk_checked.so): the global writes of the hot kernels first check
+// their index against the extent of the buffer they write; an index outside
+// it records FSK_ERR_DEVICE_BOUNDS with the call site and the write is
+// skipped (nothing traps).  In the normal build the check compiles away.
+__device__ __forceinline__ bool in_bounds(int64_t i, int64_t limit, unsigned int site) {
+#ifdef FSK_BOUNDS_CHECK
+  if (i >= 0 && i < limit) return true;
+  record_error(FSK_ERR_DEVICE_BOUNDS, site);
+  return false;
+#else
+  (void)i;
+  (void)limit;
+  (void)site;
+  return true;
+#endif
+}
+
 // This translation unit's error word, read and cleared from the host
 // (synchronous; the caller has synchronised the stream).
 static inline unsigned int take_unit_device_error() {

@@ -8,6 +8,9 @@ namespace fsk {
 unsigned int kde16_take_device_error();    // fsk_tc_kde16.cu
 unsigned int score16_take_device_error();  // fsk_tc_score16.cu
 unsigned int mlp_tc_take_device_error();   // fsk_mlp_tc.cu
+unsigned int simt_take_device_error();     // fsk_simt.cu      (bounds checks only)
+unsigned int reduce_take_device_error();   // fsk_reduce.cu    (bounds checks only)
+unsigned int logspace_take_device_error(); // fsk_logspace.cu  (bounds checks only)
 
 // ---- fsk_api.cu -------------------------------------------------------------
 // Argument checks of fsk_kde16 (pointers, sizes, bandwidth, flags and the

@@ -39,7 +39,7 @@ __global__ void reduce_rows_logexact_kernel(const double* __restrict__ partials,
     out[i] = (float)log(s * scale);
   } else {
     const uint32_t slot = atomicAdd(count, 1u);
-    list[slot] = (uint32_t)i;
+    if (in_bounds(slot, m, 56)) list[slot] = (uint32_t)i;
   }
 }
 
@@ -191,7 +191,8 @@ __global__ void logspace_combine_kernel(const uint32_t* __restrict__ count_ptr, 
       const float d = pd[(int64_t)p * m + slot];
       if (d < __int_as_float(0x7f800000)) sum += ps[(int64_t)p * m + slot] * exp2(-c2d * ((double)d - (double)dm));
     }
-    out[list[slot]] = (float)(log(sum) - c1d * (double)dm + log_scale);
+    const int64_t q = list[slot];
+    if (in_bounds(q, m, 55)) out[q] = (float)(log(sum) - c1d * (double)dm + log_scale);
   }
 }
 }  // namespace
@@ -231,5 +232,7 @@ void launch_reduce_logexact(const float* q, int64_t m, const float* x, int64_t n
                                                           out);
   count_launch();
 }
+
+unsigned int logspace_take_device_error() { return take_unit_device_error(); }
 
 }  // namespace fsk

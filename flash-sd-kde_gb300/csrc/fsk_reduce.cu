@@ -116,7 +116,8 @@ __global__ void reduce_score_w_kernel(const double* __restrict__ pw, int w_split
   for (int s = 0; s < w_splits; ++s) a += pw[(int64_t)s * n * FSK_D + e];
   const double po = p_other[i];
   const double v = self_x ? a + mu64[k] * po + (double)self_x[e] : a + mu64[k] * po;
-  w[i * ws_row + k * ws_col] = (float)v;
+  const int64_t o = i * ws_row + k * ws_col;
+  if (in_bounds(o, n * FSK_D, 53)) w[o] = (float)v;
 }
 
 size_t reduce_score_scratch_doubles(int64_t n) { return (size_t)n; }
@@ -145,7 +146,8 @@ __global__ void debias16_kernel(const float* __restrict__ x, int64_t n, const fl
 #pragma unroll
   for (int k = 0; k < FSK_D; ++k) {
     const double xi = (double)x[i * FSK_D + k];
-    const double m = (double)w[i * ws_row + k * ws_col] * inv;
+    const int64_t o = i * ws_row + k * ws_col;
+    const double m = in_bounds(o, n * FSK_D, 54) ? (double)w[o] * inv : 0.0;
     deb[i * FSK_D + k] = (float)(0.5 * (xi + m));
     if (score) score[i * FSK_D + k] = (float)((m - xi) * inv_h2);
   }
@@ -218,5 +220,7 @@ void launch_zero(double* p, int64_t count, cudaStream_t s) {
   zero_kernel<<<blocks, 256, 0, s>>>(p, count);
   count_launch();
 }
+
+unsigned int reduce_take_device_error() { return take_unit_device_error(); }
 
 }  // namespace fsk

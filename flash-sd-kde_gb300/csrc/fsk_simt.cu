@@ -92,8 +92,12 @@ __global__ void __launch_bounds__(SIMT_THREADS) kde16_simt_kernel(
     int64_t qi = q0 + threadIdx.x + u * SIMT_THREADS;
     if (!qvalid[u]) continue;
     double v = (double)acc[u].s + (double)acc[u].c;
-    if (atomic_acc) atomicAdd(&atomic_acc[qi], v);
-    else partials[(int64_t)blockIdx.y * m + qi] = v;
+    if (atomic_acc) {
+      if (in_bounds(qi, m, 44)) atomicAdd(&atomic_acc[qi], v);
+    } else {
+      const int64_t idx = (int64_t)blockIdx.y * m + qi;
+      if (in_bounds(idx, (int64_t)gridDim.y * m, 45)) partials[idx] = v;
+    }
   }
 }
 
@@ -194,8 +198,10 @@ __global__ void __launch_bounds__(SIMT_THREADS) score16_simt_kernel(
     for (int k = 0; k < FSK_D; ++k) w[k].add(wp[k]);
   }
   if (!valid_i) return;
-  ppdf[(int64_t)blockIdx.y * n + i] = (double)pdf.s + (double)pdf.c;
-  double* wo = pw + ((int64_t)blockIdx.y * n + i) * FSK_D;
+  const int64_t row = (int64_t)blockIdx.y * n + i;
+  if (in_bounds(row, (int64_t)gridDim.y * n, 46)) ppdf[row] = (double)pdf.s + (double)pdf.c;
+  if (!in_bounds(row, (int64_t)gridDim.y * n, 47)) return;   // the row's 16 features
+  double* wo = pw + row * FSK_D;
 #pragma unroll
   for (int k = 0; k < FSK_D; ++k) wo[k] = (double)w[k].s + (double)w[k].c;
 }
@@ -342,7 +348,7 @@ __global__ void __launch_bounds__(SYM_R) score16_sym_simt_kernel(
         }
         pc += e;
       }
-      if (pc != 0.f) {
+      if (pc != 0.f && in_bounds(j0 + cj, n, 48)) {
         const int64_t j = j0 + cj;
         atomicAdd(&acc_pdf[j], (double)pc);
 #pragma unroll
@@ -350,7 +356,7 @@ __global__ void __launch_bounds__(SYM_R) score16_sym_simt_kernel(
       }
     }
   }
-  if (vi) {
+  if (vi && in_bounds(i, n, 49)) {
     atomicAdd(&acc_pdf[i], (double)prow);
 #pragma unroll
     for (int k = 0; k < FSK_D; ++k) atomicAdd(&acc_w[i * FSK_D + k], (double)wrow[k]);
@@ -469,8 +475,12 @@ __global__ void __launch_bounds__(K1_THREADS) kde1d_kernel(
     int64_t qi = q0 + threadIdx.x + u * K1_THREADS;
     if (qi >= m) continue;
     double v = (double)acc[u].s + (double)acc[u].c;
-    if (atomic_acc) atomicAdd(&atomic_acc[qi], v);
-    else partials[(int64_t)blockIdx.y * m + qi] = v;
+    if (atomic_acc) {
+      if (in_bounds(qi, m, 50)) atomicAdd(&atomic_acc[qi], v);
+    } else {
+      const int64_t idx = (int64_t)blockIdx.y * m + qi;
+      if (in_bounds(idx, (int64_t)gridDim.y * m, 51)) partials[idx] = v;
+    }
   }
 }
 
@@ -550,8 +560,10 @@ __global__ void __launch_bounds__(K1_THREADS) kde1d_score_kernel(
   for (int u = 0; u < K1_Q; ++u) {
     int64_t qi = q0 + threadIdx.x + u * K1_THREADS;
     if (qi >= m) continue;
-    p0[(int64_t)blockIdx.y * m + qi] = (double)a0[u].s + (double)a0[u].c;
-    p1[(int64_t)blockIdx.y * m + qi] = (double)a1[u].s + (double)a1[u].c;
+    const int64_t idx = (int64_t)blockIdx.y * m + qi;
+    if (!in_bounds(idx, (int64_t)gridDim.y * m, 52)) continue;
+    p0[idx] = (double)a0[u].s + (double)a0[u].c;
+    p1[idx] = (double)a1[u].s + (double)a1[u].c;
   }
 }
 
@@ -565,5 +577,7 @@ void launch_kde1d_score(const float* q, int64_t m, const float* x, int64_t n, do
   kde1d_score_kernel<<<grid, K1_THREADS, 0, s>>>(q, m, x, n, nc2, tps, p0, p1);
   count_launch();
 }
+
+unsigned int simt_take_device_error() { return take_unit_device_error(); }
 
 }  // namespace fsk

@@ -368,8 +368,12 @@ __global__ void __launch_bounds__(THREADS, 1) kde16_tc_kernel(TcParams p) {
       s_carry += fabsf(acc.s + corr);
       if (gi < p.m) {
         const double v = (double)acc.s + (double)acc.c + (double)corr;
-        if (p.atomic_acc) atomicAdd(&p.atomic_acc[gi], v);
-        else p.partials[(2 * sp + half) * p.m + gi] = v;
+        if (p.atomic_acc) {
+          if (in_bounds(gi, p.m, 40)) atomicAdd(&p.atomic_acc[gi], v);
+        } else {
+          const int64_t idx = (2 * sp + half) * p.m + gi;
+          if (in_bounds(idx, 2 * p.splits * p.m, 41)) p.partials[idx] = v;
+        }
       }
       if (++sp == p.splits) {
         sp = 0;

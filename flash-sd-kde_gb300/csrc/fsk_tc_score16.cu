@@ -601,17 +601,23 @@ __global__ void __launch_bounds__(S_THREADS, 1) score16_tc_kernel(ScParams p) {
         const double p_unscale = 1.0 / 32768.0;   // 2^-PHI_LOG2_SCALE
         const double c_unscale = p_unscale;
         const double w_unscale = ldexp(p_unscale, -p.scales->pad[2]);
-        p.ppdf[(int64_t)(2 * sp + half) * p.n + gi] = ((double)acc.s + (double)acc.c + (double)corr) * p_unscale;
-        double* wrow = p.pw + ((int64_t)sp * p.n + gi) * FSK_D + half * 8;
+        const int64_t pidx = (int64_t)(2 * sp + half) * p.n + gi;
+        if (in_bounds(pidx, 2 * p.splits * p.n, 42))
+          p.ppdf[pidx] = ((double)acc.s + (double)acc.c + (double)corr) * p_unscale;
+        const int64_t wbase = ((int64_t)sp * p.n + gi) * FSK_D + half * 8;   // 8 features from here
+        const bool w_ok = in_bounds(wbase, p.splits * p.n * FSK_D - 7, 43);
+        double* wrow = p.pw + wbase;
         const float* c0 = wcorr + (k_unit & 1) * WC_PAR + wc_row + half * 8;
         const float* c1 = c0 + WC_HALF;
         const float4 s0 = wacc[threadIdx.x], s1 = wacc[EPI_T + threadIdx.x];
         const float4 e0 = wacc[2 * EPI_T + threadIdx.x], e1 = wacc[3 * EPI_T + threadIdx.x];
         const float ws[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
         const float we[8] = {e0.x, e0.y, e0.z, e0.w, e1.x, e1.y, e1.z, e1.w};
+        if (w_ok) {
 #pragma unroll
-        for (int k = 0; k < 8; ++k)
-          wrow[k] = ((double)ws[k] + (double)we[k]) * w_unscale + ((double)c0[k] + (double)c1[k]) * c_unscale;
+          for (int k = 0; k < 8; ++k)
+            wrow[k] = ((double)ws[k] + (double)we[k]) * w_unscale + ((double)c0[k] + (double)c1[k]) * c_unscale;
+        }
       }
     }
   }

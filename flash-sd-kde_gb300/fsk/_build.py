@@ -20,6 +20,12 @@ CSRC = PKG_ROOT / "csrc"
 INCLUDE = PKG_ROOT.parent / "include"
 BUILD_DIR = PKG_ROOT / "_build"
 LIB_PATH = Path(__file__).resolve().parent / "libfsk.so"
+# The bounds-check build (-DFSK_BOUNDS_CHECK: the hot kernels check their
+# global write indices and report FSK_ERR_DEVICE_BOUNDS instead of writing
+# out of range) goes to its own library and object directory.
+CHECKED_BUILD_DIR = PKG_ROOT / "_build_checked"
+CHECKED_LIB_PATH = Path(__file__).resolve().parent / "libfsk_checked.so"
+CHECKED_FLAGS = ["-DFSK_BOUNDS_CHECK"]
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
@@ -47,28 +53,32 @@ def sources() -> list[Path]:
     return sorted(CSRC.glob("*.cu"))
 
 
-def _stale(extra_flags: list[str]) -> bool:
-    if not LIB_PATH.exists():
+def _stale(extra_flags: list[str], lib_path: Path = LIB_PATH, build_dir: Path = BUILD_DIR) -> bool:
+    if not lib_path.exists():
         return True
-    stamp = BUILD_DIR / "flags.txt"
+    stamp = build_dir / "flags.txt"
     if not stamp.exists() or stamp.read_text() != " ".join(NVCC_FLAGS + extra_flags + sorted(RDC_UNITS)):
         return True
-    lib_mtime = LIB_PATH.stat().st_mtime
+    lib_mtime = lib_path.stat().st_mtime
     deps = list(CSRC.glob("*")) + list(INCLUDE.glob("*.h"))
     return any(p.stat().st_mtime > lib_mtime for p in deps)
 
 
-def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | None = None) -> Path:
-    """Compile every csrc/*.cu for sm_103a and link libfsk.so; returns its path."""
-    extra_flags = list(extra_flags or [])
-    if not force and not _stale(extra_flags):
-        return LIB_PATH
+def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | None = None,
+          checked: bool = False) -> Path:
+    """Compile every csrc/*.cu for sm_103a and link libfsk.so (checked=True:
+    the bounds-check build, libfsk_checked.so); returns the library's path."""
+    extra_flags = list(extra_flags or []) + (CHECKED_FLAGS if checked else [])
+    lib_path = CHECKED_LIB_PATH if checked else LIB_PATH
+    build_dir = CHECKED_BUILD_DIR if checked else BUILD_DIR
+    if not force and not _stale(extra_flags, lib_path, build_dir):
+        return lib_path
     nvcc = _nvcc()
-    BUILD_DIR.mkdir(exist_ok=True)
+    build_dir.mkdir(exist_ok=True)
     srcs = sources()
 
     def compile_one(src: Path) -> Path:
-        obj = BUILD_DIR / (src.stem + ".o")
+        obj = build_dir / (src.stem + ".o")
         rdc = ["-rdc=true"] if src.stem in RDC_UNITS else []
         cmd = [nvcc, *ARCH_FLAGS, *NVCC_FLAGS, *rdc, *extra_flags, f"-I{INCLUDE}", "-c", str(src), "-o", str(obj)]
         res = subprocess.run(cmd, capture_output=True, text=True)
@@ -80,18 +90,18 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
 
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(compile_one, srcs))
-    tmp = LIB_PATH.with_suffix(".so.tmp")
+    tmp = lib_path.with_suffix(".so.tmp")
     link_rdc = ["-rdc=true"] if any(o.stem in RDC_UNITS for o in objs) else []
     cmd = [nvcc, *ARCH_FLAGS, *link_rdc, "-shared", "-o", str(tmp), *map(str, objs)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
-    os.replace(tmp, LIB_PATH)
-    (BUILD_DIR / "flags.txt").write_text(" ".join(NVCC_FLAGS + extra_flags + sorted(RDC_UNITS)))
-    return LIB_PATH
+    os.replace(tmp, lib_path)
+    (build_dir / "flags.txt").write_text(" ".join(NVCC_FLAGS + extra_flags + sorted(RDC_UNITS)))
+    return lib_path
 
 
 if __name__ == "__main__":
     v = "-v" in sys.argv
     extra = ["-Xptxas", "-v"] if "--ptxas-v" in sys.argv else []
-    print(build(force=True, verbose=v or bool(extra), extra_flags=extra))
+    print(build(force=True, verbose=v or bool(extra), extra_flags=extra, checked="--checked" in sys.argv))

@@ -20,6 +20,7 @@ FSK_ERR_CUDA = 3
 FSK_ERR_DEVICE_TIMEOUT = 4
 FSK_ERR_UNSUPPORTED_DEVICE = 5
 FSK_ERR_SCRATCH_LIMIT = 6
+FSK_ERR_DEVICE_BOUNDS = 7
 
 # flags
 FSK_PREC_TENSOR = 0x0

@@ -55,7 +55,9 @@ enum fsk_status {
   FSK_ERR_CUDA = 3,               /* a CUDA runtime call failed             */
   FSK_ERR_DEVICE_TIMEOUT = 4,     /* a bounded in-kernel wait gave up       */
   FSK_ERR_UNSUPPORTED_DEVICE = 5, /* not an sm_103 device                   */
-  FSK_ERR_SCRATCH_LIMIT = 6       /* request exceeds a fixed scratch limit  */
+  FSK_ERR_SCRATCH_LIMIT = 6,      /* request exceeds a fixed scratch limit  */
+  FSK_ERR_DEVICE_BOUNDS = 7       /* bounds-check build only: a kernel index
+                                     fell outside its buffer (write skipped) */
 };
 
 /* ---- option flags ------------------------------------------------------ */
