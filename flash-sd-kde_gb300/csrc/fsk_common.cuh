@@ -212,6 +212,14 @@ __device__ __forceinline__ float exp2_neg_scaled(float dist, float c2, float c2_
   return fmaf(y, -e * 0.69314718055994531f, y);
 }
 
+// exp2_neg_scaled for two lanes with f32x2 instructions (the same roundings).
+__device__ __forceinline__ float2 exp2_neg_scaled2(float2 dist, float c2, float c2_lo) {
+  const float2 np = __fmul2_rn(dist, make_float2(-c2, -c2));                       // -p
+  const float2 e = __fadd2_rn(__ffma2_rn(dist, make_float2(c2, c2), np), __fmul2_rn(dist, make_float2(c2_lo, c2_lo)));
+  const float2 y = make_float2(ex2_approx(np.x), ex2_approx(np.y));
+  return __ffma2_rn(y, __fmul2_rn(e, make_float2(-0.69314718055994531f, -0.69314718055994531f)), y);
+}
+
 // ---- shared-memory address / mbarrier ---------------------------------------
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));

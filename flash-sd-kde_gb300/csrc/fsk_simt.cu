@@ -25,7 +25,10 @@ namespace fsk {
 // ---------------------------------------------------------------------------
 // 16-D KDE, direct differences.  Block: 128 threads x QPT queries each.
 // grid.x = query blocks, grid.y = splits; each split covers `tiles_per_split`
-// data tiles of TN points.
+// data tiles of TN points.  A thread's two queries share every f32x2
+// instruction (difference, square-accumulate, exponent, sum): the roundings
+// of the scalar code, half the issue slots (8.5e11 vs 7.9e11 pairs/s at
+// 2^20 x 2^20, bitwise the same results).
 // ---------------------------------------------------------------------------
 namespace {
 constexpr int SIMT_TN = 64;
@@ -53,6 +56,9 @@ __global__ void __launch_bounds__(SIMT_THREADS) kde16_simt_kernel(
   Comp acc[SIMT_QPT];
 #pragma unroll
   for (int u = 0; u < SIMT_QPT; ++u) acc[u] = Comp{0.f, 0.f};
+  float2 q2[FSK_D];
+#pragma unroll
+  for (int k = 0; k < FSK_D; ++k) q2[k] = make_float2(qr[0][k], qr[1][k]);
 
   const int64_t n_tiles = (n + SIMT_TN - 1) / SIMT_TN;
   const int64_t t_begin = (int64_t)blockIdx.y * tiles_per_split;
@@ -66,26 +72,30 @@ __global__ void __launch_bounds__(SIMT_THREADS) kde16_simt_kernel(
       xs[r][k] = r < valid ? x[(j0 + r) * FSK_D + k] : 0.f;
     }
     __syncthreads();
-    float part[SIMT_QPT];
-#pragma unroll
-    for (int u = 0; u < SIMT_QPT; ++u) part[u] = 0.f;
+    static_assert(SIMT_QPT == 2, "two queries per f32x2 lane pair");
+    float2 part = make_float2(0.f, 0.f);
     for (int r = 0; r < valid; ++r) {
-      float xv[FSK_D];
+      float2 s0 = make_float2(0.f, 0.f), s1 = s0, s2 = s0, s3 = s0;
 #pragma unroll
       for (int k = 0; k < FSK_D; k += 4) {
-        float4 v = *reinterpret_cast<const float4*>(&xs[r][k]);
-        xv[k] = v.x; xv[k + 1] = v.y; xv[k + 2] = v.z; xv[k + 3] = v.w;
+        const float4 v = *reinterpret_cast<const float4*>(&xs[r][k]);
+        // q - x for both queries, four features in four chains (the order of sqdist16)
+        const float2 d0 = __fadd2_rn(q2[k], make_float2(-v.x, -v.x));
+        const float2 d1 = __fadd2_rn(q2[k + 1], make_float2(-v.y, -v.y));
+        const float2 d2 = __fadd2_rn(q2[k + 2], make_float2(-v.z, -v.z));
+        const float2 d3 = __fadd2_rn(q2[k + 3], make_float2(-v.w, -v.w));
+        s0 = __ffma2_rn(d0, d0, s0);
+        s1 = __ffma2_rn(d1, d1, s1);
+        s2 = __ffma2_rn(d2, d2, s2);
+        s3 = __ffma2_rn(d3, d3, s3);
       }
-#pragma unroll
-      for (int u = 0; u < SIMT_QPT; ++u) {
-        const float dist = sqdist16(qr[u], xv);
-        float e = exp2_neg_scaled(dist, c2, c2_lo);
-        if (LAPLACE) e *= fmaf(-c1, dist, 1.0f + 0.5f * FSK_D);
-        part[u] += e;
-      }
+      const float2 dist = __fadd2_rn(__fadd2_rn(s0, s1), __fadd2_rn(s2, s3));
+      float2 e = exp2_neg_scaled2(dist, c2, c2_lo);
+      if (LAPLACE) e = __fmul2_rn(e, __ffma2_rn(make_float2(-c1, -c1), dist, make_float2(1.0f + 0.5f * FSK_D, 1.0f + 0.5f * FSK_D)));
+      part = __fadd2_rn(part, e);
     }
-#pragma unroll
-    for (int u = 0; u < SIMT_QPT; ++u) acc[u].add(part[u]);
+    acc[0].add(part.x);
+    acc[1].add(part.y);
   }
 #pragma unroll
   for (int u = 0; u < SIMT_QPT; ++u) {
