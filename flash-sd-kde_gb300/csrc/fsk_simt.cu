@@ -151,21 +151,27 @@ int simt_kde16_splits(int64_t m, int64_t n) {
 // partial pdf [split][n] and partial weighted [split][n][16].  Distances use
 // the original coordinates; the weighted sums accumulate x_j - mu (centred,
 // so the compensated FP32 sums carry the spread, not the offset) and the
-// mean is added back in FP64 by the reduction.
+// mean is added back in FP64 by the reduction.  Two data points share every
+// f32x2 instruction (the tile kept as point pairs in shared memory; even and
+// odd points in separate chains, added per tile): 2616 -> 2155 ms at 2^20.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(SIMT_THREADS) score16_simt_kernel(
     const float* __restrict__ x, int64_t n, const float* __restrict__ mu, float c2, float c2_lo,
     int64_t tiles_per_split, double* __restrict__ ppdf, double* __restrict__ pw) {
-  __shared__ __align__(16) float xs[SIMT_TN][FSK_D];
-  __shared__ __align__(16) float xcs[SIMT_TN][FSK_D];
+  // the data tile as point pairs: xs2[rp][k] = -(x_{2rp}, x_{2rp+1})[k], xcs2 the centred values
+  __shared__ __align__(16) float2 xs2[SIMT_TN / 2][FSK_D];
+  __shared__ __align__(16) float2 xcs2[SIMT_TN / 2][FSK_D];
   __shared__ float mus[FSK_D];
   if (threadIdx.x < FSK_D) mus[threadIdx.x] = mu[threadIdx.x];
   __syncthreads();
   const int64_t i = (int64_t)blockIdx.x * SIMT_THREADS + threadIdx.x;
   const bool valid_i = i < n;
-  float xi[FSK_D];
+  float2 xi2[FSK_D];
 #pragma unroll
-  for (int k = 0; k < FSK_D; ++k) xi[k] = valid_i ? x[i * FSK_D + k] : 0.f;
+  for (int k = 0; k < FSK_D; ++k) {
+    const float v = valid_i ? x[i * FSK_D + k] : 0.f;
+    xi2[k] = make_float2(v, v);
+  }
   Comp pdf{0.f, 0.f};
   Comp w[FSK_D];
 #pragma unroll
@@ -181,31 +187,43 @@ __global__ void __launch_bounds__(SIMT_THREADS) score16_simt_kernel(
     for (int e = threadIdx.x; e < SIMT_TN * FSK_D; e += SIMT_THREADS) {
       int r = e / FSK_D, k = e % FSK_D;
       const float v = r < valid ? x[(j0 + r) * FSK_D + k] : 0.f;
-      xs[r][k] = v;
-      xcs[r][k] = r < valid ? v - mus[k] : 0.f;
+      reinterpret_cast<float*>(&xs2[r >> 1][k])[r & 1] = -v;
+      reinterpret_cast<float*>(&xcs2[r >> 1][k])[r & 1] = r < valid ? v - mus[k] : 0.f;
     }
     __syncthreads();
-    float ps = 0.f;
-    float wp[FSK_D];
+    // two data points per f32x2 instruction; even and odd points in separate chains
+    float2 ps2 = make_float2(0.f, 0.f), wp2[FSK_D];
 #pragma unroll
-    for (int k = 0; k < FSK_D; ++k) wp[k] = 0.f;
-    for (int r = 0; r < valid; ++r) {
-      float xv[FSK_D], xc[FSK_D];
+    for (int k = 0; k < FSK_D; ++k) wp2[k] = make_float2(0.f, 0.f);
+    for (int rp = 0; 2 * rp < valid; ++rp) {
+      const float4* xr = reinterpret_cast<const float4*>(&xs2[rp][0]);
+      float2 d0 = make_float2(0.f, 0.f), d1 = d0, d2 = d0, d3 = d0;
 #pragma unroll
-      for (int k = 0; k < FSK_D; k += 4) {
-        float4 v = *reinterpret_cast<const float4*>(&xs[r][k]);
-        xv[k] = v.x; xv[k + 1] = v.y; xv[k + 2] = v.z; xv[k + 3] = v.w;
-        float4 c = *reinterpret_cast<const float4*>(&xcs[r][k]);
-        xc[k] = c.x; xc[k + 1] = c.y; xc[k + 2] = c.z; xc[k + 3] = c.w;
+      for (int kk = 0; kk < 4; ++kk) {
+        const float4 va = xr[2 * kk], vb = xr[2 * kk + 1];   // features 4kk, 4kk+1 | 4kk+2, 4kk+3
+        const float2 a0 = __fadd2_rn(xi2[4 * kk], make_float2(va.x, va.y));
+        const float2 a1 = __fadd2_rn(xi2[4 * kk + 1], make_float2(va.z, va.w));
+        const float2 a2 = __fadd2_rn(xi2[4 * kk + 2], make_float2(vb.x, vb.y));
+        const float2 a3 = __fadd2_rn(xi2[4 * kk + 3], make_float2(vb.z, vb.w));
+        d0 = __ffma2_rn(a0, a0, d0);
+        d1 = __ffma2_rn(a1, a1, d1);
+        d2 = __ffma2_rn(a2, a2, d2);
+        d3 = __ffma2_rn(a3, a3, d3);
       }
-      const float e = exp2_neg_scaled(sqdist16(xi, xv), c2, c2_lo);
-      ps += e;
+      float2 e = exp2_neg_scaled2(__fadd2_rn(__fadd2_rn(d0, d1), __fadd2_rn(d2, d3)), c2, c2_lo);
+      if (2 * rp + 1 >= valid) e.y = 0.f;   // the padding point of an odd tile
+      ps2 = __fadd2_rn(ps2, e);
+      const float4* xcr = reinterpret_cast<const float4*>(&xcs2[rp][0]);
 #pragma unroll
-      for (int k = 0; k < FSK_D; ++k) wp[k] = fmaf(e, xc[k], wp[k]);
+      for (int kk = 0; kk < 8; ++kk) {
+        const float4 c = xcr[kk];   // features 2kk, 2kk+1 of both points
+        wp2[2 * kk] = __ffma2_rn(e, make_float2(c.x, c.y), wp2[2 * kk]);
+        wp2[2 * kk + 1] = __ffma2_rn(e, make_float2(c.z, c.w), wp2[2 * kk + 1]);
+      }
     }
-    pdf.add(ps);
+    pdf.add(ps2.x + ps2.y);
 #pragma unroll
-    for (int k = 0; k < FSK_D; ++k) w[k].add(wp[k]);
+    for (int k = 0; k < FSK_D; ++k) w[k].add(wp2[k].x + wp2[k].y);
   }
   if (!valid_i) return;
   const int64_t row = (int64_t)blockIdx.y * n + i;
