@@ -11,6 +11,8 @@
 // DP = 16 ceil(d / 16) in registers and shared memory, which changes no
 // squared distance.  The weighted sums are accumulated centred on the FP64
 // column means (added back in the reduction), FC features per launch slice.
+// With two queries per thread (d <= 32) the KDE packs them into f32x2
+// instructions, with the roundings of the scalar code.
 #include "fsk_common.cuh"
 #include "fsk_kernels.cuh"
 
@@ -72,20 +74,47 @@ __global__ void __launch_bounds__(ND_THREADS) kde_nd_kernel(const float* __restr
     __syncthreads();
     stage_rows<DP>(xs, x, j0, valid, d);
     __syncthreads();
-    float part[QPT];
+    if constexpr (QPT == 2) {
+      // both queries in every f32x2 instruction: the roundings of the scalar
+      // code below, half the issue slots
+      float2 part = make_float2(0.f, 0.f);
+      for (int r = 0; r < valid; ++r) {
+        float2 s0 = make_float2(0.f, 0.f), s1 = s0, s2 = s0, s3 = s0;
 #pragma unroll
-    for (int u = 0; u < QPT; ++u) part[u] = 0.f;
-    for (int r = 0; r < valid; ++r) {
-#pragma unroll
-      for (int u = 0; u < QPT; ++u) {
-        const float dist = sqdist_nd<DP>(qr[u], xs[r]);
-        float e = exp2_neg_scaled(dist, c2, c2_lo);
-        if (LAPLACE) e *= fmaf(-c1, dist, lap0);
-        part[u] += e;
+        for (int k = 0; k < DP; k += 4) {
+          const float4 v = *reinterpret_cast<const float4*>(&xs[r][k]);
+          const float2 d0 = __fadd2_rn(make_float2(qr[0][k], qr[1][k]), make_float2(-v.x, -v.x));
+          const float2 d1 = __fadd2_rn(make_float2(qr[0][k + 1], qr[1][k + 1]), make_float2(-v.y, -v.y));
+          const float2 d2 = __fadd2_rn(make_float2(qr[0][k + 2], qr[1][k + 2]), make_float2(-v.z, -v.z));
+          const float2 d3 = __fadd2_rn(make_float2(qr[0][k + 3], qr[1][k + 3]), make_float2(-v.w, -v.w));
+          s0 = __ffma2_rn(d0, d0, s0);
+          s1 = __ffma2_rn(d1, d1, s1);
+          s2 = __ffma2_rn(d2, d2, s2);
+          s3 = __ffma2_rn(d3, d3, s3);
+        }
+        const float2 dist = __fadd2_rn(__fadd2_rn(s0, s1), __fadd2_rn(s2, s3));
+        float2 e = exp2_neg_scaled2(dist, c2, c2_lo);
+        if (LAPLACE) e = __fmul2_rn(e, __ffma2_rn(make_float2(-c1, -c1), dist, make_float2(lap0, lap0)));
+        part = __fadd2_rn(part, e);
       }
-    }
+      acc[0].add(part.x);
+      acc[1].add(part.y);
+    } else {
+      float part[QPT];
 #pragma unroll
-    for (int u = 0; u < QPT; ++u) acc[u].add(part[u]);
+      for (int u = 0; u < QPT; ++u) part[u] = 0.f;
+      for (int r = 0; r < valid; ++r) {
+#pragma unroll
+        for (int u = 0; u < QPT; ++u) {
+          const float dist = sqdist_nd<DP>(qr[u], xs[r]);
+          float e = exp2_neg_scaled(dist, c2, c2_lo);
+          if (LAPLACE) e *= fmaf(-c1, dist, lap0);
+          part[u] += e;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < QPT; ++u) acc[u].add(part[u]);
+    }
   }
 #pragma unroll
   for (int u = 0; u < QPT; ++u) {
