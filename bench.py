@@ -70,6 +70,83 @@ MMA_FLOPS_PER_PAIR = {"kde16_tc_kernel": {"issued": 7 * 2 * 16, "algorithmic": 2
                                             "algorithmic": 2 * 2 * 16}}
 
 
+# ---------------------------------------------------------------------------
+# FP64 spot checks of the measured outputs (self-contained: the oracle package
+# of the test suite is used only by the CPU-baseline leg)
+# ---------------------------------------------------------------------------
+def fp64_log_density(samples, queries, h: float, *, q_chunk: int = 256, s_chunk: int = 1 << 16):
+    """FP64 log-density of the Gaussian KDE, log sum_j exp(-|q - x_j|^2 / 2h^2)
+    - log n - d log h - (d/2) log 2 pi, by a chunked logsumexp; distances by
+    the FP64 expansion about the sample mean (its rounding, ~1e-16 of the
+    squared norms, is far below the FP32 errors being measured); query chunks
+    on a thread pool."""
+    import concurrent.futures as cf
+
+    import numpy as np
+
+    x = np.asarray(samples, dtype=np.float64)
+    q = np.asarray(queries, dtype=np.float64)
+    n, d = x.shape
+    c = x.mean(axis=0)
+    x, q = x - c, q - c
+    xn, qn = (x * x).sum(axis=1), (q * q).sum(axis=1)
+    log_const = -math.log(n) - d * math.log(h) - 0.5 * d * math.log(2.0 * math.pi)
+    inv2h2 = 1.0 / (2.0 * h * h)
+
+    def work(qs: int):
+        run = np.full(min(q_chunk, q.shape[0] - qs), -np.inf)
+        for ss in range(0, n, s_chunk):
+            e = q[qs:qs + q_chunk] @ x[ss:ss + s_chunk].T
+            e *= -2.0
+            e += qn[qs:qs + q_chunk, None]
+            e += xn[None, ss:ss + s_chunk]
+            np.maximum(e, 0.0, out=e)
+            e *= -inv2h2
+            mx = e.max(axis=1)
+            e -= mx[:, None]
+            np.exp(e, out=e)
+            run = np.logaddexp(run, mx + np.log(e.sum(axis=1)))
+        return run
+
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+        parts = list(ex.map(work, range(0, q.shape[0], q_chunk)))
+    return np.concatenate(parts) + log_const
+
+
+def fp64_score_rows(data, rows, h: float):
+    """FP64 (pdf_sum, weighted_sum) of the empirical score for the given data
+    rows against all points (self pair included), by direct differences."""
+    import numpy as np
+
+    x = np.asarray(data, dtype=np.float64)
+    pdf = np.zeros(len(rows))
+    w = np.zeros((len(rows), x.shape[1]))
+    for i, r in enumerate(rows):
+        phi = np.exp(-((x - x[r]) ** 2).sum(axis=1) / (2.0 * h * h))
+        pdf[i] = phi.sum()
+        w[i] = phi @ x
+    return pdf, w
+
+
+def log_error_stats(logp, ref_logp) -> dict:
+    """Log-density error statistics over the queries finite in both: finite
+    fractions, max / mean / p95 absolute and max relative log error, RMSE,
+    bias (the measures of the reference's error suite)."""
+    import numpy as np
+
+    a, b = np.asarray(logp, dtype=np.float64), np.asarray(ref_logp, dtype=np.float64)
+    ok = np.isfinite(a) & np.isfinite(b)
+    out = {"finite_fraction": float(np.isfinite(a).mean()), "finite_fraction_ref": float(np.isfinite(b).mean())}
+    if not ok.any():
+        return out
+    diff = a[ok] - b[ok]
+    ad = np.abs(diff)
+    return {**out, "max_abs_log_err": float(ad.max()), "mean_abs_log_err": float(ad.mean()),
+            "rmse_log_err": float(np.sqrt((diff * diff).mean())), "p95_abs_log_err": float(np.quantile(ad, 0.95)),
+            "bias_log_err": float(diff.mean()),
+            "max_rel_log_err": float((ad / np.maximum(np.abs(b[ok]), 1e-300)).max())}
+
+
 def log_density_errors(dens, ref_logp) -> dict:
     """Errors of densities against FP64 log-densities: the density's relative
     error, the absolute log-density error and the relative log-density error
@@ -256,8 +333,6 @@ def run_triton_leg(args) -> None:
     for mod in (ref_api, ref_k):
         if not str(Path(mod.__file__).resolve()).startswith(str(REF_DIR.resolve())):
             raise RuntimeError(f"{mod.__name__} resolved outside {REF_DIR}")
-    from oracle import fp64
-
     dev = torch.device("cuda", 0)
     n, h = args.n, float(args.h)
     gmm = wl.GMM16(seed=0)
@@ -295,10 +370,10 @@ def run_triton_leg(args) -> None:
            "source": "baseline/_ref (the reference's flash_sd_kde/, kernels/, globals.py, unmodified)",
            "workload": f"sdkde_gmm8_16d_n{n}_m{n}", "pairs_per_step": pairs, "bandwidth": h}
     sub_q = 64
-    ref_logp = fp64.log_density(x_np, q_np[:sub_q], h)
+    ref_logp = fp64_log_density(x_np, q_np[:sub_q], h)
     # FP64 debias of rows 0..63 (self pair included)
     rows = np.arange(64)
-    pdf64, w64 = fp64.empirical_score_rows(x_np, rows, h)
+    pdf64, w64 = fp64_score_rows(x_np, rows, h)
     deb64 = x_np[:64].astype(np.float64) + 0.5 * (w64 / (pdf64[:, None] + EPS) - x_np[:64])
 
     def errors(deb, kde_of_x):
@@ -448,7 +523,6 @@ def run_gpu_arm(args) -> None:
     ge.build()
     from flash_sd_kde import emp_sd_kde_fit_transform, kde_eval
     from fsk import _lib, ops
-    from oracle import fp64
 
     lib = _lib.load()
     n = args.n
@@ -556,9 +630,9 @@ def run_gpu_arm(args) -> None:
     sub = slice(0, 64)
     deb_np = deb.cpu().numpy()
     dens_np = dens.cpu().numpy().astype(np.float64)
-    ref_logp = fp64.log_density(deb_np, q_np[sub], h)
+    ref_logp = fp64_log_density(deb_np, q_np[sub], h)
     kde_err = log_density_errors(dens_np[sub], ref_logp)
-    pdf64, w64 = fp64.empirical_score_rows(x_np, np.arange(64), h)
+    pdf64, w64 = fp64_score_rows(x_np, np.arange(64), h)
     deb64 = x_np[:64].astype(np.float64) + 0.5 * (w64 / (pdf64[:, None] + EPS) - x_np[:64])
     deb_abs = float(np.abs(deb_np[:64] - deb64).max())
 
@@ -738,7 +812,6 @@ def run_precision(args) -> None:
 
     ge.build()
     from fsk import ops, workloads
-    from oracle import fp64
 
     dev = torch.device("cuda", 0)
     n = args.n
@@ -752,7 +825,7 @@ def run_precision(args) -> None:
     for f in (0.5, 1.0, 2.0):
         h = h0 * f
         norm = 1.0 / ((2 * math.pi) ** 8 * h ** 16 * n)
-        ref = fp64.log_density_gemm(x_np, q_np[sub], h)
+        ref = fp64_log_density(x_np, q_np[sub], h)
         for mode in ("tensor", "ieee", "fp16_single", "tensor_log_exact"):
             if mode == "tensor_log_exact":
                 fn = lambda: ops.kde16_sum(q, x, h, out_scale=norm, log_exact=True)
@@ -768,7 +841,7 @@ def run_precision(args) -> None:
             ops.device_status(dev)
             got = lp.cpu().numpy().astype(np.float64)[sub]
             rows.append({"h_factor": f, "h": h, "mode": mode, "ms": e0.elapsed_time(e1),
-                         **fp64.log_error_metrics(got, ref)})
+                         **log_error_stats(got, ref)})
             print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
     print(json.dumps({"op": "precision", "workload": f"student_t5_offset100_16d_n{n}_m{n}",
                       "queries_checked": int(sub.size), "silverman_h": h0, "rows": rows}), flush=True)
