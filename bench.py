@@ -175,9 +175,10 @@ def parse():
     ap.add_argument("--no-triton", action="store_true", help="leave the reference-Triton leg out")
     ap.add_argument("--triton-leg", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--triton-steps", type=int, default=3)
+    ap.add_argument("--triton-small", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--triton-ieee", action="store_true",
                     help="also time the reference's fp32_ieee path (slow: CUDA-core FP32)")
-    ap.add_argument("--h", type=float, default=None, help=argparse.SUPPRESS)
+    ap.add_argument("--h", type=str, default=None, help=argparse.SUPPRESS)
     ap.add_argument("--surrogate", action="store_true",
                     help="run only the learned-surrogate workload (C4) and print its JSON line")
     ap.add_argument("--no-surrogate", action="store_true", help="leave the surrogate object out of the bench line")
@@ -309,6 +310,32 @@ def triton_leg(n: int, h: float, steps: int, ieee: bool) -> dict:
     return res
 
 
+def triton_small_leg(hs, steps: int) -> dict:
+    """The reference's public API at the latency op's sizes, in a child
+    process (as triton_leg); hs = the bandwidths of the plain-KDE case and of
+    each SD-KDE size."""
+    if not (REF_DIR / "kernels" / "flash_sd_kde").is_dir():
+        return {"unavailable": f"reference package not present under {REF_DIR.relative_to(ROOT)}"}
+    cmd = [sys.executable, str(ROOT / "bench.py"), "--triton-leg", "--triton-small",
+           "--h", ",".join(repr(h) for h in hs), "--steps", str(steps)]
+    env = dict(os.environ)
+    if os.path.exists("/usr/local/cuda/bin/ptxas") and "TRITON_PTXAS_PATH" not in env:
+        env["TRITON_PTXAS_PATH"] = "/usr/local/cuda/bin/ptxas"
+    try:
+        res = subprocess.run(cmd, cwd=str(ROOT), capture_output=True, text=True, timeout=900, env=env)
+        out, err, rc = res.stdout, res.stderr, res.returncode
+    except subprocess.TimeoutExpired as exc:
+        out = exc.stdout.decode() if isinstance(exc.stdout, bytes) else (exc.stdout or "")
+        err, rc = "timed out after 900 s", None
+    lines = [ln for ln in out.strip().splitlines() if ln.startswith("{")]
+    if not lines:
+        return {"unavailable": f"reference Triton small-size leg failed (rc {rc}): {err.strip()[-600:]}"}
+    res = json.loads(lines[-1])
+    if rc != 0:
+        res["incomplete"] = f"rc {rc}: {err.strip()[-300:]}"
+    return res
+
+
 def run_triton_leg(args) -> None:
     """Child process: the reference's own kernels, unmodified, from
     baseline/_ref (its package directories as published), timed with CUDA
@@ -418,6 +445,68 @@ def run_triton_leg(args) -> None:
             "ms_per_step": statistics.median(ms), "step_ms": ms,
             "pair_evals_per_s": pairs / (statistics.median(ms) * 1e-3), **errors(deb, kde_x)}
         report()
+
+
+LATENCY_SIZES = ((4096, 1024), (16384, 4096), (65536, 65536))
+
+
+def latency_inputs(n: int, m: int, plain: bool):
+    """Inputs of the small-size latency cases: the plain-KDE configuration
+    (N(0, I), 4096 / 1024, seed 0) or the GMM8 SD-KDE workload at n / m."""
+    spec = __import__("importlib.util").util.spec_from_file_location("fsk_workloads", PKG / "fsk" / "workloads.py")
+    wl = __import__("importlib.util").util.module_from_spec(spec)
+    spec.loader.exec_module(wl)
+    if plain:
+        return wl.plain_kde_16d(n, m)
+    g = wl.GMM16(seed=0)
+    return g.sample(n, seed=1), g.sample(m, seed=2)
+
+
+def time_calls(fn, warm: int, reps: int, dev) -> tuple[float, float]:
+    """(device us, host us) per call: CUDA events and wall clock around reps
+    back-to-back calls after warm-up calls."""
+    import torch
+
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize(dev)
+    return 1e3 * e0.elapsed_time(e1) / reps, 1e6 * (time.perf_counter() - t0) / reps
+
+
+def run_triton_small(args) -> None:
+    """Child process: the reference's own public API, unmodified, from
+    baseline/_ref, at the small sizes of the latency op: kde_eval on the
+    plain-KDE configuration, and emp_sd_kde_fit_transform + kde_eval on the
+    GMM8 workload; bandwidths passed in by the parent so both arms use the
+    same h."""
+    sys.path[:] = [str(REF_DIR)] + [p for p in sys.path if p not in (str(PKG), str(ROOT))] + [str(ROOT)]
+    import torch
+
+    import flash_sd_kde as ref_api
+    if not str(Path(ref_api.__file__).resolve()).startswith(str(REF_DIR.resolve())):
+        raise RuntimeError(f"flash_sd_kde resolved outside {REF_DIR}")
+    dev = torch.device("cuda", 0)
+    hs = [float(v) for v in args.h.split(",")]
+    rows = []
+    x_np, q_np = latency_inputs(4096, 1024, plain=True)
+    x, q = torch.from_numpy(x_np).to(dev), torch.from_numpy(q_np).to(dev)
+    us, host = time_calls(lambda: ref_api.kde_eval(x, q, hs[0], device=dev), 5, max(10, args.steps), dev)
+    rows.append({"case": "plain_kde", "n_train": 4096, "n_query": 1024, "kde_eval_us": us, "kde_eval_host_us": host})
+    for (n, m), h in zip(LATENCY_SIZES, hs[1:]):
+        x_np, q_np = latency_inputs(n, m, plain=False)
+        x, q = torch.from_numpy(x_np).to(dev), torch.from_numpy(q_np).to(dev)
+        fn = lambda: ref_api.kde_eval(ref_api.emp_sd_kde_fit_transform(x, h, device=dev), q, h, device=dev)
+        us, host = time_calls(fn, 5, max(10, args.steps), dev)
+        rows.append({"case": "sdkde", "n_train": n, "n_query": m, "two_calls_us": us, "two_calls_host_us": host})
+        print(json.dumps({"impl": "reference-triton", "rows": rows}), flush=True)
+    print(json.dumps({"impl": "reference-triton", "rows": rows}), flush=True)
 
 
 # ---------------------------------------------------------------------------
@@ -863,18 +952,28 @@ def run_sdkde_latency(args) -> None:
 
     dev = torch.device("cuda", 0)
     rows = []
-    for n, m in ((4096, 1024), (16384, 4096), (65536, 65536)):
+    hs = []
+    # the plain-KDE configuration (4096 N(0, I) points, 1024 queries): the public kde_eval
+    x_np, q_np = latency_inputs(4096, 1024, plain=True)
+    x, q = torch.from_numpy(x_np).to(dev), torch.from_numpy(q_np).to(dev)
+    h = float(ops.silverman(x).item())
+    hs.append(h)
+    us, host = time_calls(lambda: kde_eval(x, q, h, device=dev), 5, max(10, args.steps), dev)
+    rows.append({"case": "plain_kde", "n_train": 4096, "n_query": 1024, "kde_eval_us": us, "kde_eval_host_us": host})
+    print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
+    for n, m in LATENCY_SIZES:
         g = workloads.GMM16(seed=0)
         x = torch.from_numpy(g.sample(n, seed=1)).to(dev)
         q = torch.from_numpy(g.sample(m, seed=2)).to(dev)
         h = float(ops.silverman(x).item())
+        hs.append(h)
         graph = ops.SDKDEGraph(x, q, h)
         ws = ops._workspace(ops.L.load().fsk_sdkde16_workspace_bytes(n, m, 0), dev)
         out = torch.empty(m, dtype=torch.float32, device=dev)
         fns = {"two_calls": lambda: kde_eval(emp_sd_kde_fit_transform(x, h, device=dev), q, h, device=dev),
                "one_call": lambda: ops.sdkde16(x, q, h, out=out, workspace=ws),
                "graph_replay": graph.replay}
-        row = {"n_train": n, "n_query": m}
+        row = {"case": "sdkde", "n_train": n, "n_query": m}
         for name, fn in fns.items():
             for _ in range(max(3, args.warmup)):
                 fn()
@@ -892,7 +991,10 @@ def run_sdkde_latency(args) -> None:
         ops.device_status(dev)
         rows.append(row)
         print(json.dumps(row), file=sys.stderr, flush=True)
-    print(json.dumps({"op": "sdkde_latency", "rows": rows}), flush=True)
+    ref = None
+    if not args.no_triton:
+        ref = triton_small_leg(hs, args.steps)
+    print(json.dumps({"op": "sdkde_latency", "rows": rows, "reference_triton": ref}), flush=True)
 
 
 def run_op(args) -> None:
@@ -979,7 +1081,10 @@ def _time_op(args, dev, fn, pairs, h) -> None:
 def main():
     args = parse()
     if args.triton_leg:
-        run_triton_leg(args)
+        if args.triton_small:
+            run_triton_small(args)
+        else:
+            run_triton_leg(args)
         return
     if args.op:
         run_op(args)
