@@ -453,8 +453,10 @@ LATENCY_SIZES = ((4096, 1024), (16384, 4096), (65536, 65536))
 def latency_inputs(n: int, m: int, plain: bool):
     """Inputs of the small-size latency cases: the plain-KDE configuration
     (N(0, I), 4096 / 1024, seed 0) or the GMM8 SD-KDE workload at n / m."""
-    spec = __import__("importlib.util").util.spec_from_file_location("fsk_workloads", PKG / "fsk" / "workloads.py")
-    wl = __import__("importlib.util").util.module_from_spec(spec)
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("fsk_workloads", PKG / "fsk" / "workloads.py")
+    wl = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(wl)
     if plain:
         return wl.plain_kde_16d(n, m)
